@@ -1,0 +1,407 @@
+#!/usr/bin/env python
+"""Sparse FFTs per second at n=2^27, k=16000 on GB300: mixed vs FP64.
+
+Workload (one step = one sparse FFT, the reference's outer_loop): n = 2^27,
+k = 16000, Bcst = 0.65, loops_loc = 2, loops_thresh = 2, loops_est = 7,
+RLFC_cst = 4096, RLFC_loops = 2, filter tolerance 1e-8; seeded synthetic
+signal (unit-magnitude, uniform-phase coefficients at distinct uniform
+locations, noiseless); a fresh set of random draws (RLFC offsets, sigma) per
+step.  The signal (1 GiB FP32 / 2 GiB FP64) is larger than L2, so no flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gsfft|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the oracle,
+OpenMP on all host cores): the reference itself has no CPU path.  Under
+torchrun every rank runs an independent replica (the path does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "gpu-sfft_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+CFG = dict(q=27, k=16000, Bcst=0.65, loops_loc=2, loops_thresh=2, loops_est=7, RLFC_cst=4096,
+           RLFC_loops=2)
+METRIC = "sparse FFTs/sec at n=2^27,k=16000: mixed vs FP64 on 1 GB300 at <=1e-5 rel L2"
+UNIT = "sparse FFTs/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def cfg_args(cfg):
+    return (cfg["q"], cfg["k"], cfg["Bcst"], cfg["loops_loc"], cfg["loops_thresh"],
+            cfg["loops_est"], cfg["RLFC_cst"], cfg["RLFC_loops"])
+
+
+def workload_config(cfg, extra=None):
+    d = {"workload": f"sfft n=2^{cfg['q']} k={cfg['k']} Bcst={cfg['Bcst']} loops={cfg['loops_loc']}"
+                     f"/{cfg['loops_thresh']}/{cfg['loops_est']} RLFC={cfg['RLFC_cst']}x"
+                     f"{cfg['RLFC_loops']} tol=1e-8 noiseless",
+         "l2": "inputs_larger_than_l2", "parallelism": "replicas"}
+    d.update(extra or {})
+    return d
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"])}, "measured"
+    except Exception:
+        return dict(PEAKS_FALLBACK), "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ----------------------------------------------------------------------------
+# reference arm: the oracle (CPU restatement of the reference algorithm)
+# ----------------------------------------------------------------------------
+
+def cpu_signal(n, k, seed):
+    from gsfft import synth
+    loc, coef = synth.sparse_spectrum(n, k, seed)
+    X = np.zeros(n, np.complex128)
+    X[loc] = coef
+    try:
+        import scipy.fft as sf
+        x = sf.ifft(X, workers=-1) * n
+    except Exception:
+        x = np.fft.ifft(X) * n
+    return x, loc, coef
+
+
+def run_reference(args, cfg):
+    ws, rank, _ = dist_init()
+    if rank != 0:
+        return 0
+    from gsfft import synth
+    from oracle import oracle as O
+    p, st = O.derive_params(*cfg_args(cfg))
+    assert st == 0
+    t0 = time.perf_counter()
+    x, loc, coef = cpu_signal(p.n, p.k, 0)
+    ft, ff = O.design_filter(p)
+    setup_s = time.perf_counter() - t0
+    draws = [synth.draws(s, p.n, p.W_RLFC, p.RLFC_loops, p.loops) for s in range(args.warmup + args.steps)]
+    for s in range(args.warmup):
+        O.outer_loop(x, p, ft, ff, *draws[s])
+    t0 = time.perf_counter()
+    res = None
+    for s in range(args.steps):
+        res = O.outer_loop(x, p, ft, ff, *draws[args.warmup + s])
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    top = O.topk(res["nodes"], p.k)
+    cores = O.oc_num_threads() if hasattr(O, "oc_num_threads") else O.lib().oc_num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(cfg, {"setup_s_untimed": round(setup_s, 2)}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full sparse FFTs (oracle/sfft_oracle.c, OpenMP, "
+                                   f"{cores} threads) after {args.warmup} warm-up runs"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "accuracy": {"missed_topk": int(len(set(loc.tolist()) - set(top["key"].tolist())))},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+
+def stage_bytes(p, es):
+    """Algorithmic bytes per launch of each single-stage measurement."""
+    L, w, B, W, R = p.loops, p.w, p.B, p.W_RLFC, p.RLFC_loops
+    t = es // 2
+    return {
+        # every tap of every loop gathers one signal element, taps read once, bins written once
+        "perm_filter": L * w * es + w * es + L * B * es,
+        # strided gather of W samples per RLFC loop + |.|^2 written; 2 passes through scratch
+        "rlfc_fft": R * W * es + R * W * t + 2 * R * W * es,
+        "bucket_fft": 2 * L * B * es * 2 + L * B * t,
+    }
+
+
+def run_ours(args, cfg):
+    import torch
+    import gsfft
+    from gsfft import synth
+
+    ws, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    gsfft.lib()  # fail loudly if the CUDA library was not built
+    p, st = gsfft.derive_params(*cfg_args(cfg))
+    assert st == 0, st
+    n, k = p.n, p.k
+    dev = torch.device("cuda", local)
+    # --- untimed setup: signal, filter, plans
+    x64, loc, coef, _X = synth.signal_torch(n, k, seed=rank, device=dev)
+    del _X
+    torch.cuda.synchronize()
+    d_ft = torch.zeros(p.w, dtype=torch.complex128, device=dev)
+    d_ff = torch.zeros(n, dtype=torch.complex128, device=dev)
+    t0 = time.perf_counter()
+    gsfft.design_filter(p, d_ft.data_ptr(), d_ff.data_ptr())
+    torch.cuda.synchronize()
+    filter_ms = (time.perf_counter() - t0) * 1e3
+    x32 = x64.to(torch.complex64)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    plans = {"fp64": gsfft.Plan(p, gsfft.FP64), "mixed": gsfft.Plan(p, gsfft.MIXED)}
+    for pl in plans.values():
+        pl.set_filter(d_ft.data_ptr(), d_ff.data_ptr(), sh)
+    xin = {"fp64": x64, "mixed": x32}
+    total = args.warmup + args.steps
+    draws = [synth.draws(1000 * rank + s, n, p.W_RLFC, p.RLFC_loops, p.loops) for s in range(total)]
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(name, sampler=None):
+        pl, xx = plans[name], xin[name]
+        for s in range(args.warmup):
+            pl.run(xx.data_ptr(), *draws[s], stream=sh)
+        pl.enable_timing(True)
+        barrier()
+        if sampler:
+            sampler.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(args.steps):
+            pl.run(xx.data_ptr(), *draws[args.warmup + s], stream=sh)
+        e1.record(stream)
+        barrier()
+        clocks = sampler.stop() if sampler else None
+        ms = e0.elapsed_time(e1)
+        stages, runs = pl.stage_times()
+        pl.enable_timing(False)
+        if dist:
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, stages, clocks
+
+    ms64, st64, _ = timed("fp64")
+    sampler = ClockSampler(local)
+    ms32, st32, clocks = timed("mixed", sampler)
+
+    # --- accuracy: same signal and draws through both paths
+    acc = {}
+    last = draws[-1]
+    res = {}
+    for name in ("fp64", "mixed"):
+        plans[name].run(xin[name].data_ptr(), *last, stream=sh)
+        res[name] = plans[name].results(stream=sh)
+    k64 = res["fp64"]["topk"]["key"].tolist()
+    k32 = res["mixed"]["topk"]["key"].tolist()
+    v64 = dict(zip(k64, res["fp64"]["topk"]["x"] + 1j * res["fp64"]["topk"]["y"]))
+    common = [kk for kk in k32 if kk in v64]
+    v32 = {kk: complex(r["x"], r["y"]) for kk, r in zip(k32, res["mixed"]["topk"])}
+    a64 = np.array([v64[kk] for kk in common])
+    a32 = np.array([v32[kk] for kk in common])
+    truth = dict(zip(loc.tolist(), coef))
+    t64 = np.array([truth.get(kk, 0) for kk in k64])
+    acc = {
+        "same_location_set": set(k64) == set(k32),
+        "mixed_vs_fp64_rel_l2": float(np.linalg.norm(a32 - a64) / max(np.linalg.norm(a64), 1e-300)),
+        "fp64_missed_vs_truth": int(len(set(loc.tolist()) - set(k64))),
+        "fp64_vs_full_fft_rel_l2": float(np.linalg.norm(
+            (res["fp64"]["topk"]["x"] + 1j * res["fp64"]["topk"]["y"]) - t64) / np.sqrt(k)),
+        "I_F": res["fp64"]["I_F"],
+    }
+
+    # --- end to end through the C ABI with host buffers (mixed path)
+    h_x = torch.empty(n, dtype=torch.complex64, pin_memory=True)
+    h_x.copy_(x32)
+    d_in = torch.empty_like(x32)
+    pl = plans["mixed"]
+    h2d = n * 8
+    d2h = k * 24 + 8
+    for s in range(min(2, args.warmup)):
+        d_in.copy_(h_x, non_blocking=True)
+        pl.run(d_in.data_ptr(), *draws[s], stream=sh)
+        pl.results(stream=sh)
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        d_in.copy_(h_x, non_blocking=True)
+        pl.run(d_in.data_ptr(), *draws[args.warmup + s], stream=sh)
+        pl.results(stream=sh)  # device -> host copy of the k largest + counts (synchronises)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    # --- roofline of the dominant single-kernel stage of the mixed run
+    peaks, peak_src = load_peaks()
+    sb = stage_bytes(p, 8)
+    dom = max(("perm_filter", "rlfc_fft", "bucket_fft"), key=lambda s: st32.get(s, 0.0))
+    achieved = sb[dom] / (st32[dom] * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get(dom)
+        except Exception:
+            traffic = None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+            "peak": peaks["hbm_gbs"], "peak_source": peak_src, "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+            "algorithmic_bytes_per_launch": sb[dom], "launch_ms": round(st32[dom], 4)}
+
+    # --- CPU baseline (rank 0): the oracle on the host cores, bounded sample
+    cpu = None
+    if rank == 0 and not args.skip_cpu_baseline:
+        from oracle import oracle as O
+        po, _ = O.derive_params(*cfg_args(cfg))
+        hx = x64.cpu().numpy()
+        hft, hff = d_ft.cpu().numpy(), d_ff.cpu().numpy()
+        O.outer_loop(hx, po, hft, hff, *draws[0])
+        reps, t0 = 0, time.perf_counter()
+        while reps < 3 or (time.perf_counter() - t0 < 10.0 and reps < 20):
+            O.outer_loop(hx, po, hft, hff, *draws[1 + reps % (total - 1)])
+            reps += 1
+        cdt = time.perf_counter() - t0
+        cores = O.lib().oc_num_threads()
+        cpu = {"value": reps / cdt, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{reps} full sparse FFTs of this workload, oracle/sfft_oracle.c with "
+                         f"{cores} OpenMP threads"}
+
+    launches = plans["mixed"].launches_per_run() * args.steps
+    value = ws * args.steps / (ms32 * 1e-3)
+    fp64 = ws * args.steps / (ms64 * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16/f64-estimate (mixed)",
+        "data": "synthetic",
+        "config": workload_config(cfg, {"global_batch": ws, "filter_design_ms_untimed":
+                                        round(filter_ms, 1)}),
+        "fp64": {"value": fp64, "unit": UNIT, "ms_per_step": ms64 / args.steps,
+                 "stage_ms": {kk: round(v, 4) for kk, v in st64.items()}},
+        "mixed_over_fp64": value / fp64,
+        "stage_ms": {kk: round(v, 4) for kk, v in st32.items()},
+        "accuracy": acc,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": ws * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for pl in plans.values():
+        pl.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gsfft", choices=["gsfft", "reference"])
+    ap.add_argument("--q", type=int, default=None, help=argparse.SUPPRESS)  # smaller n for local checks
+    ap.add_argument("--skip-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    cfg = dict(CFG)
+    if args.q is not None:
+        cfg.update(q=args.q, k=1000, Bcst=1.40, loops_est=5, RLFC_cst=128)
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,331 @@
+// Plan and run orchestration: the outer loop of outerLoop.cu:65-190 as one
+// stream-ordered sequence of kernels with every buffer allocated at plan time.
+//
+// Data layout in HBM (T = double in FP64 mode, float in MIXED mode):
+//   x            n complex T (caller)             signal
+//   filt         w complex T                      filter taps
+//   hinv         n/B + 1 complex double           conj(H)/|H|^2 around bin 0
+//   rsamp        RLFC_loops x W_RLFC T            |FFT_W(restricted x)|^2
+//   J2b / J2     RLFC_loops x B_thresh int        RLFC blocks / merged ids
+//   bins         loops x B complex T              bucket spectra (in place FFT)
+//   bsamp        loops x B T                      |bins|^2
+//   J            loops_loc x B_thresh int         heavy buckets per location loop
+//   bm_j2, bm_sig  W/32 and loops_loc x W/32 u32  residue bitmaps
+//   vote         n u32                            epoch << 8 | count
+//   cand, nodes, mag2, topk_idx, topk             candidate list and results
+#include "engine.cuh"
+
+#include <stdlib.h>
+#include <string.h>
+
+namespace gsfft {
+
+namespace {
+
+__global__ void convert_taps_kernel(const double2 *__restrict__ src, void *dst, int w, int to_float) {
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= w) return;
+  const double2 v = src[i];
+  if (to_float) reinterpret_cast<float2 *>(dst)[i] = make_float2((float)v.x, (float)v.y);
+  else reinterpret_cast<double2 *>(dst)[i] = v;
+}
+
+// hinv[idx] = conj(H)/|H|^2 with H = filter_freq[(n - d) mod n], d = idx - nb/2
+__global__ void hinv_kernel(const double2 *__restrict__ ff, int n, int nb, double2 *hinv) {
+  const int idx = blockIdx.x * 256 + threadIdx.x;
+  if (idx > nb) return;
+  const int d = idx - nb / 2;
+  const int dist = (int)(((long long)n - d) & (long long)(n - 1));
+  const double2 H = ff[dist];
+  const double a2 = __dadd_rn(__dmul_rn(H.x, H.x), __dmul_rn(H.y, H.y));
+  hinv[idx] = make_double2(H.x / a2, -H.y / a2);
+}
+
+template <typename P> int alloc(P **p, size_t bytes) {
+  cudaError_t e = cudaMalloc((void **)p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    set_last_error("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    return GSFFT_ERR_ALLOC;
+  }
+  return GSFFT_OK;
+}
+
+}  // namespace
+
+int validate_params(const gsfft_params &p) {
+  auto pow2 = [](long long v) { return v > 0 && (v & (v - 1)) == 0; };
+  if (!pow2(p.n) || p.n < 256 || p.n > (1 << 30)) return GSFFT_ERR_PARAM;
+  if (!pow2(p.B) || p.B > p.n || !pow2(p.W_RLFC) || p.W_RLFC > p.n) return GSFFT_ERR_PARAM;
+  if (p.B_thresh < 1 || p.B_thresh >= p.B || p.B_thresh >= p.W_RLFC) return GSFFT_ERR_PARAM;
+  if (p.loops_loc < 1 || p.loops_thresh < 1 || p.loops_thresh > p.loops_loc) return GSFFT_ERR_PARAM;
+  if (p.loops != p.loops_loc + p.loops_est || p.loops > MAX_LOOPS || p.loops_loc > 255)
+    return GSFFT_ERR_PARAM;
+  if (p.RLFC_loops < 1 || p.RLFC_loops > MAX_RLFC_LOOPS) return GSFFT_ERR_PARAM;
+  if (p.w < 1 || p.w > p.n) return GSFFT_ERR_PARAM;
+  // the window of a bucket must be shorter than W_RLFC, and W_RLFC < n
+  if (p.W_RLFC >= p.n || p.W_RLFC <= p.n / p.B || p.W_RLFC < 256) return GSFFT_ERR_UNSUPPORTED;
+  if (p.B < 256) return GSFFT_ERR_UNSUPPORTED;
+  return GSFFT_OK;
+}
+
+int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_candidates,
+                Plan **out) {
+  *out = nullptr;
+  GS_CHECK(validate_params(pp));
+  if (precision != GSFFT_FP64 && precision != GSFFT_MIXED) return GSFFT_ERR_PARAM;
+  Plan *P = new Plan();
+  P->p = pp;
+  P->precision = precision;
+  P->flags = flags;
+  P->cap = max_candidates > 0 ? max_candidates : 524288;
+  const gsfft_params &p = P->p;
+  const size_t T = precision == GSFFT_FP64 ? 8 : 4, V = 2 * T;
+  P->es = V;
+  int s = GSFFT_OK;
+  const int nb = p.n / p.B;
+  const size_t wW = (size_t)p.W_RLFC / 32;
+#define A(ptr, bytes) \
+  if (s == GSFFT_OK) s = alloc(&P->ptr, (bytes))
+  A(filt, V * p.w);
+  A(hinv, sizeof(double2) * (nb + 1));
+  A(rsamp, T * (size_t)p.RLFC_loops * p.W_RLFC);
+  A(J2b, sizeof(int) * (size_t)p.RLFC_loops * p.B_thresh);
+  A(J2, sizeof(int) * (size_t)p.RLFC_loops * p.B_thresh);
+  A(bins, V * (size_t)p.loops * p.B);
+  A(bsamp, T * (size_t)p.loops * p.B);
+  A(J, sizeof(int) * (size_t)p.loops_loc * p.B_thresh);
+  A(bm_j2, sizeof(unsigned) * wW);
+  A(bm_sig, sizeof(unsigned) * wW * p.loops_loc);
+  A(tile_tmp, sizeof(unsigned) * (wW / 2048 + 2));
+  A(vote, sizeof(unsigned) * (size_t)p.n);
+  A(cand, sizeof(int) * (size_t)P->cap);
+  A(cnt, sizeof(int) * (size_t)p.B_thresh);
+  A(blk, sizeof(int) * (size_t)(p.B_thresh / 256 + 2));
+  A(nodes, sizeof(DevNode) * (size_t)P->cap);
+  A(mag2, sizeof(double) * (size_t)P->cap);
+  A(topk_idx, sizeof(int) * (size_t)p.k + 16);
+  A(topk, sizeof(DevNode) * (size_t)p.k + 16);
+  A(ctl, sizeof(RunCtl));
+#undef A
+  if (s == GSFFT_OK) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
+  if (s == GSFFT_OK) s = fft_plan_init(P->fftW, p.W_RLFC, precision, p.RLFC_loops);
+  if (s == GSFFT_OK) s = select_scratch_init(P->selB, p.loops_loc, p.B);
+  if (s == GSFFT_OK) s = select_scratch_init(P->selW, p.RLFC_loops, p.W_RLFC);
+  if (s == GSFFT_OK) s = select_scratch_init(P->selK, 1, P->cap);
+  if (s == GSFFT_OK) {
+    cudaError_t e = cudaMemset(P->vote, 0, sizeof(unsigned) * (size_t)p.n);
+    if (e == cudaSuccess) e = cudaMemset(P->ctl, 0, sizeof(RunCtl));
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+      set_last_error("plan init: %s", cudaGetErrorString(e));
+      s = GSFFT_ERR_CUDA;
+    }
+  }
+  if (s != GSFFT_OK) {
+    plan_destroy(P);
+    return s;
+  }
+  P->epoch = 0;
+  *out = P;
+  return GSFFT_OK;
+}
+
+void plan_destroy(Plan *P) {
+  if (!P) return;
+  void *ptrs[] = {P->filt, P->hinv, P->rsamp, P->J2b, P->J2, P->bins, P->bsamp, P->J,
+                  P->bm_j2, P->bm_sig, P->tile_tmp, P->vote, P->cand, P->cnt, P->blk,
+                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  for (cudaEvent_t e : P->events) cudaEventDestroy(e);
+  fft_plan_free(P->fftB);
+  fft_plan_free(P->fftW);
+  select_scratch_free(P->selB);
+  select_scratch_free(P->selW);
+  select_scratch_free(P->selK);
+  delete P;
+}
+
+int launch_hinv(const double2 *d_ff, int n, int nb, double2 *hinv, cudaStream_t st) {
+  hinv_kernel<<<(nb + 1 + 255) / 256, 256, 0, st>>>(d_ff, n, nb, hinv);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+int launch_convert_taps(const double2 *d_ft, void *dst, int w, bool to_float, cudaStream_t st) {
+  convert_taps_kernel<<<(w + 255) / 256, 256, 0, st>>>(d_ft, dst, w, to_float ? 1 : 0);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+int plan_set_filter(Plan *P, const void *d_ft, const void *d_ff, cudaStream_t st) {
+  const gsfft_params &p = P->p;
+  if (!d_ft || !d_ff) return GSFFT_ERR_PARAM;
+  GS_CHECK(launch_convert_taps((const double2 *)d_ft, P->filt, p.w, P->precision == GSFFT_MIXED, st));
+  GS_CHECK(launch_hinv((const double2 *)d_ff, p.n, p.n / p.B, P->hinv, st));
+  GS_CUDA(cudaStreamSynchronize(st));
+  P->filter_set = true;
+  return GSFFT_OK;
+}
+
+int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int *ai,
+             cudaStream_t st) {
+  if (!P->filter_set) return GSFFT_ERR_STATE;
+  const gsfft_params &p = P->p;
+  const int before = g_launch_counter;
+  Draws d;
+  memset(&d, 0, sizeof(d));
+  for (int r = 0; r < p.RLFC_loops; r++) {
+    if (offs[r] < 0 || offs[r] >= p.n / p.W_RLFC) return GSFFT_ERR_PARAM;
+    d.offs[r] = offs[r];
+  }
+  for (int l = 0; l < p.loops; l++) {
+    if ((a[l] & 1) == 0 || (ai[l] & 1) == 0 || a[l] <= 0 || ai[l] <= 0 || a[l] >= p.n || ai[l] >= p.n)
+      return GSFFT_ERR_PARAM;
+    d.a[l] = a[l];
+    d.ai[l] = ai[l];
+  }
+  // epoch-tagged vote table: clear only when the 24-bit epoch wraps
+  P->epoch++;
+  if (P->epoch >= (1u << 24)) {
+    GS_CUDA(cudaMemsetAsync(P->vote, 0, sizeof(unsigned) * (size_t)p.n, st));
+    P->epoch = 1;
+  }
+  GS_CUDA(cudaMemsetAsync(P->ctl, 0, sizeof(RunCtl), st));
+  const int kb = P->precision == GSFFT_FP64 ? 8 : 4;
+  cudaEvent_t *ev = nullptr;
+  if (P->timing && P->timed_runs < 512) {
+    const size_t need = (size_t)(P->timed_runs + 1) * (ST_COUNT + 1);
+    while (P->events.size() < need) {
+      cudaEvent_t e;
+      GS_CUDA(cudaEventCreate(&e));
+      P->events.push_back(e);
+    }
+    ev = &P->events[(size_t)P->timed_runs * (ST_COUNT + 1)];
+    P->timed_runs++;
+  }
+#define MARK(i) \
+  if (ev) GS_CUDA(cudaEventRecord(ev[i], st))
+  MARK(0);
+
+  // A4: RLFC -- strided gather fused into the first FFT pass, |.|^2 epilogue
+  {
+    FftIo io;
+    io.gather_x = d_x;
+    for (int r = 0; r < p.RLFC_loops; r++) io.gather_offsets[r] = d.offs[r];
+    io.gather_stride = p.n / p.W_RLFC;
+    io.samples = P->rsamp;
+    io.write_complex = false;
+    GS_CHECK(fft_exec(P->fftW, nullptr, P->rsamp, p.RLFC_loops, -1, io, st));
+    MARK(1);
+    GS_CHECK(select_top(P->rsamp, kb, p.W_RLFC, nullptr, p.B_thresh, p.RLFC_loops, p.W_RLFC,
+                        P->J2b, p.B_thresh, nullptr, P->selW, st));
+    MARK(2);
+    GS_CHECK(launch_j2_merge(P->J2b, p.RLFC_loops * p.B_thresh, p.W_RLFC, P->bm_j2, P->J2, P->ctl,
+                             P->tile_tmp, st));
+    GS_CHECK(launch_sigma_bitmaps(P->J2, P->ctl, p.RLFC_loops * p.B_thresh, p.W_RLFC,
+                                  p.loops_loc, d, P->bm_sig, P->ctl, st));
+  }
+  MARK(3);
+  // A5 + A6: perm+filter for every loop, bucket FFT, cutoff of location loops
+  GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d,
+                              (P->flags & GSFFT_FLAG_QUIRK_RESIDUE) != 0, P->bins, st));
+  MARK(4);
+  {
+    FftIo io;
+    io.samples = P->bsamp;
+    GS_CHECK(fft_exec(P->fftB, P->bins, P->bins, p.loops, -1, io, st));
+  }
+  MARK(5);
+  GS_CHECK(select_top(P->bsamp, kb, p.B, nullptr, p.B_thresh, p.loops_loc, p.B, P->J, p.B_thresh,
+                      nullptr, P->selB, st));
+  MARK(6);
+  // A7: voting, one location loop after the other
+  const size_t wW = (size_t)p.W_RLFC / 32;
+  for (int l = 0; l < p.loops_loc; l++)
+    GS_CHECK(launch_vote_loop(l, P->J + (size_t)l * p.B_thresh, p.B_thresh, p.n, p.B, p.W_RLFC,
+                              P->bm_sig + wW * l, d, p.loops_thresh, P->epoch, P->vote, P->cand,
+                              P->cap, P->cnt, P->blk, P->ctl, st));
+  MARK(7);
+  // A8: estimation; A9: k largest
+  GS_CHECK(launch_estimate(P->precision, P->cand, P->ctl, P->cap, P->bins, p.loops, p.n, p.B, d,
+                           P->hinv, P->nodes, P->mag2, st));
+  MARK(8);
+  GS_CHECK(select_top(P->mag2, 8, P->cap, &P->ctl->cand_count, p.k, 1, P->cap, P->topk_idx, p.k,
+                      &P->ctl->n_topk, P->selK, st));
+  GS_CHECK(launch_gather_nodes(P->nodes, P->topk_idx, &P->ctl->n_topk, p.k, P->topk, st));
+  MARK(9);
+#undef MARK
+  P->launches_per_run = g_launch_counter - before;
+  P->ran = true;
+  return GSFFT_OK;
+}
+
+int plan_results(Plan *P, Node *h_nodes, int nodes_cap, int *I_F, Node *h_topk, int topk_cap,
+                 int *n_topk, cudaStream_t st) {
+  if (!P->ran) return GSFFT_ERR_STATE;
+  RunCtl c;
+  GS_CUDA(cudaMemcpyAsync(&c, P->ctl, sizeof(RunCtl), cudaMemcpyDeviceToHost, st));
+  GS_CUDA(cudaStreamSynchronize(st));
+  const int count = c.cand_count < P->cap ? c.cand_count : P->cap;
+  if (I_F) *I_F = c.cand_count;
+  if (h_nodes && nodes_cap > 0) {
+    const int m = count < nodes_cap ? count : nodes_cap;
+    if (m > 0) GS_CUDA(cudaMemcpy(h_nodes, P->nodes, sizeof(Node) * m, cudaMemcpyDeviceToHost));
+  }
+  if (n_topk) *n_topk = c.n_topk;
+  if (h_topk && topk_cap > 0) {
+    const int m = c.n_topk < topk_cap ? c.n_topk : topk_cap;
+    if (m > 0) GS_CUDA(cudaMemcpy(h_topk, P->topk, sizeof(Node) * m, cudaMemcpyDeviceToHost));
+  }
+  return c.overflow ? GSFFT_ERR_CAPACITY : GSFFT_OK;
+}
+
+const char *stage_name(int i) {
+  static const char *names[ST_COUNT] = {"rlfc_fft", "rlfc_select", "j2_merge", "perm_filter",
+                                        "bucket_fft", "cutoff", "vote", "estimate", "topk"};
+  return (i >= 0 && i < ST_COUNT) ? names[i] : "";
+}
+
+int plan_enable_timing(Plan *P, bool on) {
+  P->timing = on;
+  P->timed_runs = 0;
+  return GSFFT_OK;
+}
+
+int plan_stage_times(Plan *P, float *ms_avg, int max_stages, int *runs) {
+  GS_CUDA(cudaDeviceSynchronize());
+  const int R = P->timed_runs;
+  if (runs) *runs = R;
+  for (int sidx = 0; sidx < ST_COUNT && sidx < max_stages; sidx++) {
+    double acc = 0.0;
+    for (int r = 0; r < R; r++) {
+      float ms = 0.f;
+      cudaEvent_t *e = &P->events[(size_t)r * (ST_COUNT + 1)];
+      GS_CUDA(cudaEventElapsedTime(&ms, e[sidx], e[sidx + 1]));
+      acc += ms;
+    }
+    ms_avg[sidx] = R ? (float)(acc / R) : 0.f;
+  }
+  P->timed_runs = 0;
+  return GSFFT_OK;
+}
+
+int plan_debug(Plan *P, int *h_J2, int *num_RLFC, int *h_J, void *h_bins, cudaStream_t st) {
+  if (!P->ran) return GSFFT_ERR_STATE;
+  const gsfft_params &p = P->p;
+  GS_CUDA(cudaStreamSynchronize(st));
+  RunCtl c;
+  GS_CUDA(cudaMemcpy(&c, P->ctl, sizeof(RunCtl), cudaMemcpyDeviceToHost));
+  if (num_RLFC) *num_RLFC = c.num_rlfc;
+  if (h_J2 && c.num_rlfc > 0)
+    GS_CUDA(cudaMemcpy(h_J2, P->J2, sizeof(int) * c.num_rlfc, cudaMemcpyDeviceToHost));
+  if (h_J)
+    GS_CUDA(cudaMemcpy(h_J, P->J, sizeof(int) * (size_t)p.loops_loc * p.B_thresh,
+                       cudaMemcpyDeviceToHost));
+  if (h_bins)
+    GS_CUDA(cudaMemcpy(h_bins, P->bins, P->es * (size_t)p.loops * p.B, cudaMemcpyDeviceToHost));
+  return GSFFT_OK;
+}
+
+}  // namespace gsfft

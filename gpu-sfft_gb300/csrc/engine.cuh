@@ -1,0 +1,67 @@
+// Plan object and orchestration entry points.
+#pragma once
+#include "stages.cuh"
+
+#include <vector>
+
+namespace gsfft {
+
+enum Stage {
+  ST_RLFC_FFT = 0, ST_RLFC_SELECT, ST_J2, ST_PERM_FILTER, ST_BUCKET_FFT, ST_CUTOFF, ST_VOTE,
+  ST_ESTIMATE, ST_TOPK, ST_COUNT
+};
+
+struct Plan {
+  gsfft_params p;
+  int precision = 0;
+  unsigned flags = 0;
+  int cap = 0;
+  size_t es = 16;
+  bool filter_set = false;
+  bool ran = false;
+  unsigned epoch = 0;
+  int launches_per_run = 0;
+  FftPlan fftB, fftW;
+  SelectScratch selB, selW, selK;
+  void *filt = nullptr;
+  double2 *hinv = nullptr;
+  void *rsamp = nullptr;
+  int *J2b = nullptr, *J2 = nullptr;
+  void *bins = nullptr, *bsamp = nullptr;
+  int *J = nullptr;
+  unsigned *bm_j2 = nullptr, *bm_sig = nullptr, *tile_tmp = nullptr;
+  unsigned *vote = nullptr;
+  int *cand = nullptr, *cnt = nullptr, *blk = nullptr;
+  DevNode *nodes = nullptr;
+  double *mag2 = nullptr;
+  int *topk_idx = nullptr;
+  DevNode *topk = nullptr;
+  RunCtl *ctl = nullptr;
+  // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
+  bool timing = false;
+  std::vector<cudaEvent_t> events;  // (ST_COUNT + 1) per recorded run
+  int timed_runs = 0;
+};
+
+int validate_params(const gsfft_params &p);
+int plan_create(const gsfft_params &p, int precision, unsigned flags, int max_candidates,
+                Plan **out);
+void plan_destroy(Plan *P);
+int plan_set_filter(Plan *P, const void *d_filter_time, const void *d_filter_freq,
+                    cudaStream_t st);
+int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int *ai,
+             cudaStream_t st);
+int plan_results(Plan *P, Node *h_nodes, int nodes_cap, int *I_F, Node *h_topk, int topk_cap,
+                 int *n_topk, cudaStream_t st);
+int plan_enable_timing(Plan *P, bool on);
+int plan_stage_times(Plan *P, float *ms_avg, int max_stages, int *runs);
+const char *stage_name(int i);
+int plan_debug(Plan *P, int *h_J2, int *num_RLFC, int *h_J, void *h_bins, cudaStream_t st);
+
+int launch_hinv(const double2 *d_ff, int n, int nb, double2 *hinv, cudaStream_t st);
+int launch_convert_taps(const double2 *d_ft, void *dst, int w, bool to_float, cudaStream_t st);
+
+// A2 filter design on the GPU
+int design_filter(const gsfft_params &p, double2 *d_ft, double2 *d_ff, cudaStream_t st);
+
+}  // namespace gsfft

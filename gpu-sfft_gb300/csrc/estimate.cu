@@ -1,0 +1,101 @@
+// A8: per-candidate value estimate (estimate_values, innerLoop.cu:396-466;
+// estimateValuesKernel, :825-870) and the A9 gather of the top-k nodes.
+//
+// The reference allocates two arrays with device malloc in every thread and
+// insertion-sorts them; here each thread keeps its loops' values in local
+// arrays and picks the median by rank.  For loop j:
+//   p = ai_j * loc mod n, h = p / (n/B), d = p mod (n/B);
+//   if d > (n/B)/2 then h = (h + 1) mod B, d -= n/B;          (innerLoop.cu:838-845)
+//   v_j = bins_j[h] * conj(H[(n - d) mod n]) / |H[(n - d) mod n]|^2
+// The reciprocal response conj(H)/|H|^2 is precomputed in FP64 for the n/B + 1
+// offsets d the formula can produce, so the estimate is one complex multiply
+// in FP64 per loop (bins are promoted from FP32 in the mixed path).  The
+// median of the real parts and of the imaginary parts is taken separately,
+// element (loops-1)/2 of the ascending order (:855-861).
+#include "stages.cuh"
+
+namespace gsfft {
+
+namespace {
+
+constexpr int ET = 128;
+
+__device__ __forceinline__ double median_of(const double *v, int L) {
+  const int want = (L - 1) / 2;
+  double res = v[0];
+  for (int i = 0; i < L; i++) {
+    int rank = 0;
+    for (int j = 0; j < L; j++) rank += (v[j] < v[i]) || (v[j] == v[i] && j < i);
+    if (rank == want) res = v[i];
+  }
+  return res;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(ET)
+estimate_kernel(const int *__restrict__ cand, const RunCtl *ctl, int cap,
+                const typename Cx<T>::V *__restrict__ bins, int loops, unsigned nmask, int lognb,
+                int B, Draws d, const double2 *__restrict__ hinv, DevNode *nodes, double *mag2) {
+  const int i = blockIdx.x * ET + threadIdx.x;
+  const int count = min(ctl->cand_count, cap);
+  if (i >= count) return;
+  const unsigned loc = (unsigned)cand[i];
+  const int nb = 1 << lognb;
+  double vr[MAX_LOOPS], vi[MAX_LOOPS];
+  for (int j = 0; j < loops; j++) {
+    const unsigned p = ((unsigned)d.ai[j] * loc) & nmask;
+    int h = (int)(p >> lognb);
+    int dd = (int)(p & (unsigned)(nb - 1));
+    if (dd > nb / 2) {
+      h = (h + 1) & (B - 1);
+      dd -= nb;
+    }
+    const double2 H = hinv[dd + nb / 2];
+    const typename Cx<T>::V bv = bins[(size_t)j * B + h];
+    const double bx = (double)bv.x, by = (double)bv.y;
+    vr[j] = fma(bx, H.x, -(by * H.y));
+    vi[j] = fma(bx, H.y, by * H.x);
+  }
+  const double re = median_of(vr, loops), im = median_of(vi, loops);
+  DevNode nd;
+  nd.key = loc;
+  nd.pad = 0;
+  nd.x = re;
+  nd.y = im;
+  nodes[i] = nd;
+  mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+}
+
+__global__ void gather_nodes_kernel(const DevNode *__restrict__ nodes, const int *__restrict__ idx,
+                                    const int *count, int cap, DevNode *out) {
+  const int k = blockIdx.x * 256 + threadIdx.x;
+  if (k < min(*count, cap)) out[k] = nodes[idx[k]];
+}
+
+}  // namespace
+
+int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, const void *bins,
+                    int loops, int n, int B, const Draws &d, const double2 *hinv, DevNode *nodes,
+                    double *mag2, cudaStream_t st) {
+  int lognb = 0;
+  while ((1 << lognb) < n / B) lognb++;
+  const unsigned nmask = (unsigned)n - 1u;
+  const int grid = (cap + ET - 1) / ET;
+  if (precision == GSFFT_FP64)
+    estimate_kernel<double><<<grid, ET, 0, st>>>(cand, ctl, cap, (const double2 *)bins, loops,
+                                                 nmask, lognb, B, d, hinv, nodes, mag2);
+  else
+    estimate_kernel<float><<<grid, ET, 0, st>>>(cand, ctl, cap, (const float2 *)bins, loops, nmask,
+                                                lognb, B, d, hinv, nodes, mag2);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+int launch_gather_nodes(const DevNode *nodes, const int *idx, const int *count, int cap,
+                        DevNode *out, cudaStream_t st) {
+  gather_nodes_kernel<<<(cap + 255) / 256, 256, 0, st>>>(nodes, idx, count, cap, out);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+}  // namespace gsfft

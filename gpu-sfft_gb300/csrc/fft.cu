@@ -1,0 +1,380 @@
+// Power-of-two complex FFT for sm_103a, FP64 and FP32, batched.
+//
+// Replaces the cuFFT Z2Z plans of the reference (innerLoop.cu:144-152 for the
+// W_RLFC-point RLFC transform, :252-256 for the B-point bucket transform,
+// cuExperiment.cu:305-308 / :362-365 / :425-426 for the filter design).
+//
+// Algorithm: Stockham auto-sort with one large radix R = 2^LOGR per global
+// pass (1 pass up to 2^13 (FP64) / 2^14 (FP32) points, 2 passes up to 2^24,
+// 3 passes beyond).  Pass p with Ns = product of the earlier radices:
+//   v[r] = in[j + r*N/R] * exp(-2 pi i (j mod Ns) r / (Ns R));  V = DFT_R(v);
+//   out[(j / Ns) Ns R + (j mod Ns) + k Ns] = V[k]
+// Each CTA runs G sub-transforms of size R in shared memory as a Stockham
+// sequence of radix-16 register stages (one radix-2/4/8 stage for the
+// remainder).  G >= 2 (FP64) / 4 (FP32) so every strided global access moves
+// whole 32-byte sectors.  Twiddles come from exact-angle tables (sincospi in
+// FP64), never from recurrences.  Inverse = conj(DFT(conj(x))).
+#include "gsfft_internal.cuh"
+
+#include <algorithm>
+
+namespace gsfft {
+
+namespace {
+
+// cos / sin of 2 pi m / 16
+__device__ __forceinline__ double c16d(int m) {
+  const double t[8] = {1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173,
+                       0.0, -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613};
+  return t[m];
+}
+__device__ __forceinline__ double s16d(int m) {
+  const double t[8] = {0.0, 0.38268343236508977173, 0.70710678118654752440, 0.92387953251128675613,
+                       1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173};
+  return t[m];
+}
+
+// a * exp(-2 pi i m / 16), m in [0, 8) (compile-time after unrolling)
+template <typename V> __device__ __forceinline__ V tw16(V a, int m) {
+  typedef decltype(a.x) T;
+  if (m == 0) return a;
+  if (m == 4) { V r; r.x = a.y; r.y = -a.x; return r; }
+  T c = (T)c16d(m), s = (T)s16d(m);
+  V r;
+  r.x = fma(a.x, c, a.y * s);
+  r.y = fma(a.y, c, -(a.x * s));
+  return r;
+}
+
+template <int E> __device__ __forceinline__ constexpr int bitrev(int k) {
+  int r = 0;
+  for (int b = 1; b < E; b <<= 1) { r = (r << 1) | (k & 1); k >>= 1; }
+  return r;
+}
+
+// In-register forward DFT of E = 2,4,8,16 points (radix-2 DIF); the result
+// X[k] is left in v[bitrev(k)].
+template <typename V, int E> __device__ __forceinline__ void dft_reg(V *v) {
+#pragma unroll
+  for (int half = E / 2; half >= 1; half >>= 1) {
+#pragma unroll
+    for (int blk = 0; blk < E; blk += 2 * half) {
+#pragma unroll
+      for (int j = 0; j < half; j++) {
+        V a = v[blk + j], b = v[blk + j + half];
+        v[blk + j] = cadd(a, b);
+        v[blk + j + half] = tw16(csub(a, b), j * (8 / half));
+      }
+    }
+  }
+}
+
+__host__ __device__ constexpr int imin(int a, int b) { return a < b ? a : b; }
+__host__ __device__ constexpr int imax(int a, int b) { return a > b ? a : b; }
+
+// sub-transforms per CTA
+template <typename T> __host__ __device__ constexpr int g_of(int logr);
+template <> __host__ __device__ constexpr int g_of<double>(int logr) {
+  return logr >= 13 ? 1 : imax(2, 2048 >> logr);
+}
+template <> __host__ __device__ constexpr int g_of<float>(int logr) {
+  return logr >= 14 ? 1 : (logr == 13 ? 2 : imax(4, 4096 >> logr));
+}
+template <typename T> __host__ __device__ constexpr int nt_of(int logr) {
+  return imin(((1 << logr) / 16) * g_of<T>(logr), 512);
+}
+__host__ __device__ constexpr int padded(int i) { return i + (i >> 4); }
+template <typename T> __host__ __device__ constexpr int smem_of(int logr) {
+  return g_of<T>(logr) * padded(1 << logr) * (int)sizeof(typename Cx<T>::V);
+}
+
+// One Stockham stage of radix E inside shared memory, for all G rows.
+template <typename V, int LOGR, int G, int E>
+__device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR, int Ns) {
+  constexpr int R = 1 << LOGR;
+  constexpr int RP = padded(R);
+  constexpr int NT = imin((R / 16) * G, 512);
+  constexpr int TPF = NT / G;
+  constexpr int NB = R / E;          // butterflies per row
+  constexpr int Q = NB / TPF;        // butterflies per thread
+  const int g = threadIdx.x / TPF, t0 = threadIdx.x % TPF;
+  V *s = sm + g * RP;
+  V v[Q][E];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int t = t0 + q * TPF;
+#pragma unroll
+    for (int e = 0; e < E; e++) v[q][e] = s[padded(t + e * NB)];
+    if (Ns > 1) {
+      const int k = t % Ns;
+      const int step = R / (Ns * E);
+#pragma unroll
+      for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], twR[k * e * step]);
+    }
+    dft_reg<V, E>(v[q]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int t = t0 + q * TPF;
+    const int base = (t / Ns) * Ns * E + (t % Ns);
+#pragma unroll
+    for (int e = 0; e < E; e++) s[padded(base + e * Ns)] = v[q][bitrev<E>(e)];
+  }
+  __syncthreads();
+}
+
+template <typename V, int LOGR, int G>
+__device__ __forceinline__ void cta_fft(V *sm, const V *__restrict__ twR) {
+  constexpr int LEFT = LOGR % 4;
+  int Ns = 1;
+  if (LEFT == 1) { smem_stage<V, LOGR, G, 2>(sm, twR, Ns); Ns <<= 1; }
+  if (LEFT == 2) { smem_stage<V, LOGR, G, 4>(sm, twR, Ns); Ns <<= 2; }
+  if (LEFT == 3) { smem_stage<V, LOGR, G, 8>(sm, twR, Ns); Ns <<= 3; }
+#pragma unroll 1
+  for (int s = 0; s < LOGR / 4; s++) { smem_stage<V, LOGR, G, 16>(sm, twR, Ns); Ns <<= 4; }
+}
+
+struct PassArgs {
+  const void *in;
+  void *out;
+  long long N;        // transform size
+  long long bstride;  // batch stride of in/out/samples (elements)
+  int batch;
+  long long total;    // sub-transforms over the whole batch
+  int Ns;
+  int inverse;
+  const void *tw_hi, *tw_lo;
+  int tw_h;
+  const void *twR;
+  const void *gx;     // gather source (first pass only) or null
+  long long goffs[8];
+  long long gstride;
+  void *samples;      // last pass only, or null
+  int write_complex;
+};
+
+__device__ __forceinline__ double sq_sum(double2 v) { return __dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)); }
+__device__ __forceinline__ float sq_sum(float2 v) { return __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)); }
+
+template <typename T, int LOGR>
+__global__ void __launch_bounds__(nt_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
+  typedef typename Cx<T>::V V;
+  constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = padded(R);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V *sm = reinterpret_cast<V *>(smraw);
+  const V *__restrict__ in = reinterpret_cast<const V *>(a.in);
+  const V *__restrict__ gx = reinterpret_cast<const V *>(a.gx);
+  const V *__restrict__ thi = reinterpret_cast<const V *>(a.tw_hi);
+  const V *__restrict__ tlo = reinterpret_cast<const V *>(a.tw_lo);
+  const long long S = a.N / R;
+  const long long u0 = (long long)blockIdx.x * G;
+  const int hmask = (1 << a.tw_h) - 1;
+  for (int lt = threadIdx.x; lt < R * G; lt += NT) {
+    int g, r;
+    if (S >= G) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+    const long long u = u0 + g;
+    const long long b = u / S, j = u - b * S;
+    const long long m = j + (long long)r * S;
+    V v;
+    if (u >= a.total) v = mk((T)0, (T)0);
+    else if (gx) v = gx[a.goffs[b] + m * a.gstride];
+    else v = in[b * a.bstride + m];
+    if (a.inverse) v.y = -v.y;
+    if (a.Ns > 1) {
+      const long long mm = (j % a.Ns) * r;  // < Ns * R
+      V w = cmul(thi[mm >> a.tw_h], tlo[mm & hmask]);
+      v = cmul(v, w);
+    }
+    sm[g * RP + padded(r)] = v;
+  }
+  __syncthreads();
+  cta_fft<V, LOGR, G>(sm, reinterpret_cast<const V *>(a.twR));
+  V *__restrict__ out = reinterpret_cast<V *>(a.out);
+  T *__restrict__ smp = reinterpret_cast<T *>(a.samples);
+  for (int lt = threadIdx.x; lt < R * G; lt += NT) {
+    int g, k;
+    if (a.Ns >= G) { g = lt % G; k = lt / G; } else { k = lt % R; g = lt / R; }
+    const long long u = u0 + g;
+    if (u >= a.total) continue;
+    const long long b = u / S, j = u - b * S;
+    const long long dest = (j / a.Ns) * a.Ns * R + (j % a.Ns) + (long long)k * a.Ns;
+    V v = sm[g * RP + padded(k)];
+    if (a.inverse) v.y = -v.y;
+    if (a.write_complex) out[b * a.bstride + dest] = v;
+    if (smp) smp[b * a.bstride + dest] = sq_sum(v);
+  }
+}
+
+// exp(-2 pi i m / Np) for m in [0, count) at spacing `mul`
+template <typename V>
+__global__ void twiddle_table_kernel(V *t, long long count, long long mul, long long Np) {
+  long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= count) return;
+  double s, c;
+  // angle 2*pi*(m*mul)/Np, reduced exactly in integers
+  long long num = (m * mul) % Np;
+  sincospi(2.0 * (double)num / (double)Np, &s, &c);
+  t[m].x = (decltype(t[m].x))c;
+  t[m].y = (decltype(t[m].y))(-s);
+}
+
+template <typename T>
+int make_table(void **dst, long long count, long long mul, long long Np) {
+  typedef typename Cx<T>::V V;
+  GS_CUDA(cudaMalloc(dst, sizeof(V) * count));
+  twiddle_table_kernel<V><<<(unsigned)((count + 255) / 256), 256>>>((V *)*dst, count, mul, Np);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+template <typename T, int LOGR>
+int launch_pass(const PassArgs &a, long long total_sub, cudaStream_t st) {
+  constexpr int G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), SM = smem_of<T>(LOGR);
+  static bool attr_done = false;  // per instantiation; idempotent if raced
+  if (!attr_done) {
+    GS_CUDA(cudaFuncSetAttribute(fft_pass_kernel<T, LOGR>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+    attr_done = true;
+  }
+  long long grid = (total_sub + G - 1) / G;
+  if (grid > 0x7fffffffLL) return GSFFT_ERR_UNSUPPORTED;
+  fft_pass_kernel<T, LOGR><<<(unsigned)grid, NT, SM, st>>>(a);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+template <typename T>
+int dispatch_pass(int logr, const PassArgs &a, long long total_sub, cudaStream_t st) {
+  switch (logr) {
+    case 7: return launch_pass<T, 7>(a, total_sub, st);
+    case 8: return launch_pass<T, 8>(a, total_sub, st);
+    case 9: return launch_pass<T, 9>(a, total_sub, st);
+    case 10: return launch_pass<T, 10>(a, total_sub, st);
+    case 11: return launch_pass<T, 11>(a, total_sub, st);
+    case 12: return launch_pass<T, 12>(a, total_sub, st);
+    case 13: return launch_pass<T, 13>(a, total_sub, st);
+    case 14:
+      if constexpr (sizeof(T) == 4) return launch_pass<T, 14>(a, total_sub, st);
+      break;
+    default: break;
+  }
+  return GSFFT_ERR_UNSUPPORTED;
+}
+
+}  // namespace
+
+int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch) {
+  fft_plan_free(p);
+  if (n < 256 || (n & (n - 1)) != 0) return GSFFT_ERR_UNSUPPORTED;
+  int L = 0;
+  while ((1LL << L) < n) L++;
+  const int one_pass_max = precision == GSFFT_FP64 ? 13 : 14;
+  p.n = n;
+  p.L = L;
+  p.precision = precision;
+  if (L <= one_pass_max) {
+    p.npass = 1;
+    p.logR[0] = L;
+  } else if (L <= 24) {
+    p.npass = 2;
+    p.logR[0] = (L + 1) / 2;
+    p.logR[1] = L - p.logR[0];
+  } else if (L <= 36) {
+    p.npass = 3;
+    p.logR[0] = (L + 2) / 3;
+    p.logR[1] = (L - p.logR[0] + 1) / 2;
+    p.logR[2] = L - p.logR[0] - p.logR[1];
+  } else {
+    return GSFFT_ERR_UNSUPPORTED;
+  }
+  for (int i = 0; i < p.npass; i++)
+    if (p.logR[i] < 7 || p.logR[i] > one_pass_max) return GSFFT_ERR_UNSUPPORTED;
+  const bool dbl = precision == GSFFT_FP64;
+  long long Np = 1;
+  for (int i = 0; i < p.npass; i++) {
+    const long long R = 1LL << p.logR[i];
+    Np *= R;
+    int lg = 0;
+    while ((1LL << lg) < Np) lg++;
+    const int h = (lg + 1) / 2;
+    p.tw_h[i] = h;
+    const long long nlo = 1LL << h, nhi = (Np + nlo - 1) / nlo;
+    if (dbl) {
+      GS_CHECK(make_table<double>(&p.tw_lo[i], nlo, 1, Np));
+      GS_CHECK(make_table<double>(&p.tw_hi[i], nhi, nlo, Np));
+      GS_CHECK(make_table<double>(&p.tw_R[i], R, 1, R));
+    } else {
+      GS_CHECK(make_table<float>(&p.tw_lo[i], nlo, 1, Np));
+      GS_CHECK(make_table<float>(&p.tw_hi[i], nhi, nlo, Np));
+      GS_CHECK(make_table<float>(&p.tw_R[i], R, 1, R));
+    }
+  }
+  if (p.npass > 1) {
+    const size_t es = dbl ? 16 : 8;
+    p.scratch_elems = (long long)n * max_batch * (p.npass == 3 ? 2 : 1);
+    GS_CUDA(cudaMalloc(&p.scratch, es * p.scratch_elems));
+  }
+  GS_CUDA(cudaDeviceSynchronize());
+  return GSFFT_OK;
+}
+
+void fft_plan_free(FftPlan &p) {
+  for (int i = 0; i < 3; i++) {
+    if (p.tw_hi[i]) cudaFree(p.tw_hi[i]);
+    if (p.tw_lo[i]) cudaFree(p.tw_lo[i]);
+    if (p.tw_R[i]) cudaFree(p.tw_R[i]);
+    p.tw_hi[i] = p.tw_lo[i] = p.tw_R[i] = nullptr;
+  }
+  if (p.scratch) cudaFree(p.scratch);
+  p.scratch = nullptr;
+  p.npass = 0;
+}
+
+int fft_launches(const FftPlan &p) { return p.npass; }
+
+int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
+             const FftIo &io, cudaStream_t st) {
+  if (p.npass == 0) return GSFFT_ERR_STATE;
+  const bool dbl = p.precision == GSFFT_FP64;
+  const size_t es = dbl ? 16 : 8;
+  if (p.npass > 1 && (long long)batch * p.n * (p.npass == 3 ? 2 : 1) > p.scratch_elems)
+    return GSFFT_ERR_PARAM;
+  if (io.gather_x && batch > 8) return GSFFT_ERR_PARAM;
+  const void *src = in;
+  char *scr = (char *)p.scratch;
+  long long Ns = 1;
+  for (int i = 0; i < p.npass; i++) {
+    const bool last = i == p.npass - 1;
+    void *dst;
+    if (last) dst = out;
+    else dst = scr + (size_t)(i == 1 ? 1 : 0) * es * p.n * batch;
+    PassArgs a;
+    a.in = src;
+    a.out = dst;
+    a.N = p.n;
+    a.bstride = p.n;
+    a.batch = batch;
+    a.Ns = (int)Ns;
+    a.inverse = sign > 0;
+    a.tw_hi = p.tw_hi[i];
+    a.tw_lo = p.tw_lo[i];
+    a.tw_h = p.tw_h[i];
+    a.twR = p.tw_R[i];
+    a.gx = (i == 0) ? io.gather_x : nullptr;
+    for (int q = 0; q < 8; q++) a.goffs[q] = io.gather_offsets[q];
+    a.gstride = io.gather_stride;
+    a.samples = last ? io.samples : nullptr;
+    a.write_complex = last ? (io.write_complex ? 1 : 0) : 1;
+    const long long total_sub = (p.n >> p.logR[i]) * batch;
+    a.total = total_sub;
+    int s = dbl ? dispatch_pass<double>(p.logR[i], a, total_sub, st)
+                : dispatch_pass<float>(p.logR[i], a, total_sub, st);
+    if (s != GSFFT_OK) return s;
+    src = dst;
+    Ns <<= p.logR[i];
+  }
+  return GSFFT_OK;
+}
+
+}  // namespace gsfft

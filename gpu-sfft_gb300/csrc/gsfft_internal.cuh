@@ -1,0 +1,125 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "gsfft.h"
+
+namespace gsfft {
+
+// ---------------------------------------------------------------- errors
+void set_last_error(const char *fmt, ...);
+
+#define GS_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      ::gsfft::set_last_error("%s:%d %s: %s", __FILE__, __LINE__, #call,     \
+                              cudaGetErrorString(e_));                       \
+      return GSFFT_ERR_CUDA;                                                 \
+    }                                                                        \
+  } while (0)
+
+#define GS_CHECK(call)                        \
+  do {                                        \
+    int s_ = (call);                          \
+    if (s_ != GSFFT_OK) return s_;            \
+  } while (0)
+
+// Every kernel launch goes through this: checks the launch and counts it.
+extern thread_local int g_launch_counter;
+#define GS_LAUNCHED()                                                         \
+  do {                                                                        \
+    ++::gsfft::g_launch_counter;                                              \
+    cudaError_t e_ = cudaGetLastError();                                      \
+    if (e_ != cudaSuccess) {                                                  \
+      ::gsfft::set_last_error("%s:%d launch: %s", __FILE__, __LINE__,         \
+                              cudaGetErrorString(e_));                        \
+      return GSFFT_ERR_CUDA;                                                  \
+    }                                                                         \
+  } while (0)
+
+// ---------------------------------------------------------------- complex
+template <typename T> struct Cx;
+template <> struct Cx<double> { typedef double2 V; };
+template <> struct Cx<float> { typedef float2 V; };
+
+__host__ __device__ __forceinline__ double2 mk(double x, double y) { return make_double2(x, y); }
+__host__ __device__ __forceinline__ float2 mk(float x, float y) { return make_float2(x, y); }
+
+template <typename V> __device__ __forceinline__ V cadd(V a, V b) { V c; c.x = a.x + b.x; c.y = a.y + b.y; return c; }
+template <typename V> __device__ __forceinline__ V csub(V a, V b) { V c; c.x = a.x - b.x; c.y = a.y - b.y; return c; }
+template <typename V> __device__ __forceinline__ V cconj(V a) { a.y = -a.y; return a; }
+// (a.x b.x - a.y b.y, a.x b.y + a.y b.x), two fused operations per component.
+template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
+  V c;
+  c.x = fma(a.x, b.x, -(a.y * b.y));
+  c.y = fma(a.x, b.y, a.y * b.x);
+  return c;
+}
+
+// Keys whose unsigned order equals the order of non-negative floats.
+template <typename T> struct KeyOf;
+template <> struct KeyOf<double> { typedef unsigned long long K; };
+template <> struct KeyOf<float> { typedef unsigned int K; };
+
+// ---------------------------------------------------------------- FFT
+struct FftPlan {
+  long long n = 0;         // transform size (power of two)
+  int L = 0;               // log2 n
+  int precision = 0;       // GSFFT_FP64 / GSFFT_MIXED (float)
+  int npass = 0;
+  int logR[3] = {0, 0, 0}; // radix of each pass (log2)
+  // per pass: twiddle tables for exp(-2 pi i m / Np) with Np = prod radices
+  // up to and including the pass, split as hi[m >> h] * lo[m & (2^h - 1)].
+  void *tw_hi[3] = {nullptr, nullptr, nullptr};
+  void *tw_lo[3] = {nullptr, nullptr, nullptr};
+  int tw_h[3] = {0, 0, 0};
+  void *tw_R[3] = {nullptr, nullptr, nullptr};  // exp(-2 pi i m / R) for the pass radix
+  void *scratch = nullptr; // one transform-sized buffer per batch entry (multi-pass)
+  long long scratch_elems = 0;
+};
+
+// Optional fused prologue/epilogue of an FFT execution.
+struct FftIo {
+  // gather loader (first pass): element m of batch b is x[offs[b] + m * stride]
+  const void *gather_x = nullptr;
+  long long gather_offsets[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // one per batch entry (batch <= 8)
+  long long gather_stride = 0;
+  // epilogue: |X|^2 (same precision) written to samples[b * n + k]
+  void *samples = nullptr;
+  bool write_complex = true;
+};
+
+int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch);
+void fft_plan_free(FftPlan &p);
+// in: batch entries at in + b*n; out: out + b*n.  sign -1 forward, +1 inverse.
+int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
+             const FftIo &io, cudaStream_t st);
+int fft_launches(const FftPlan &p);
+
+// ---------------------------------------------------------------- select
+// Top-`num` of each row by key (ties at the threshold: lowest index first),
+// indices written ascending.  keys: double or float samples (bit patterns of
+// non-negative values).  size either fixed (size_dev == nullptr) or read from
+// *size_dev (rows then have capacity `size`, only the first *size_dev used;
+// batch must be 1).  When the live size <= num, all live indices are taken.
+struct SelectScratch {
+  void *hist = nullptr;        // batch * 2048 uint32
+  void *state = nullptr;       // batch * SelState
+  void *tiles = nullptr;       // batch * max_tiles * 2 uint32
+  int max_batch = 0, max_tiles = 0;
+};
+int select_scratch_init(SelectScratch &s, int max_batch, long long max_size);
+void select_scratch_free(SelectScratch &s);
+int select_top(const void *keys, int key_bytes, long long size, const int *size_dev,
+               int num, int batch, long long row_stride, int *out, long long out_stride,
+               int *count_out, SelectScratch &s, cudaStream_t st);
+int select_launches(int key_bytes);
+
+// ---------------------------------------------------------------- misc kernels
+int launch_grid(long long threads, int block);
+
+}  // namespace gsfft

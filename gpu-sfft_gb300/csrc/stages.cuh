@@ -1,0 +1,64 @@
+// Stage kernels of the sparse-FFT pipeline (launch helpers).
+#pragma once
+#include "gsfft_internal.cuh"
+
+namespace gsfft {
+
+constexpr int MAX_LOOPS = 32;
+constexpr int MAX_RLFC_LOOPS = 8;
+
+// Random draws of one run, passed by value to the kernels that need them.
+struct Draws {
+  int offs[MAX_RLFC_LOOPS];  // RLFC offsets (innerLoop.cu:123)
+  int a[MAX_LOOPS];          // sigma (outerLoop.cu:131)
+  int ai[MAX_LOOPS];         // sigma^-1 mod n (outerLoop.cu:133)
+};
+
+// Device-side state of one run.
+struct RunCtl {
+  int cand_count;      // candidates appended so far (may exceed capacity)
+  int overflow;        // set when cand_count > capacity
+  int num_rlfc;        // |J2|
+  int n_topk;
+  int fmax[MAX_LOOPS]; // largest permuted residue per location loop
+  unsigned ticket;
+  int pad[3];
+};
+
+struct DevNode {  // == Node (utils.h:42-45)
+  unsigned key;
+  unsigned pad;
+  double x, y;
+};
+
+// A5: bins[l][b] = sum_{id=b+jB<w} x[(id*ai_l) mod n] * filt[id]  (all loops)
+int launch_perm_filter(int precision, const void *x, int n, const void *filt, int w, int B,
+                       int loops, const Draws &d, bool quirk_residue, void *bins, cudaStream_t st);
+
+// J2 = sorted distinct union of the RLFC blocks, through a W-bit bitmap.
+int launch_j2_merge(const int *J2_blocks, int total, int W, unsigned *bitmap, int *J2,
+                    RunCtl *ctl, unsigned *tile_tmp, cudaStream_t st);
+int j2_merge_launches();
+
+// Permuted-residue bitmaps F_l = {J2[m] * ai_l mod W} for the location loops,
+// and fmax_l = max F_l.
+int launch_sigma_bitmaps(const int *J2, const RunCtl *ctl_num, int max_num, int W, int loops_loc,
+                         const Draws &d, unsigned *bitmaps, RunCtl *ctl, cudaStream_t st);
+
+// A7: one location loop of voting; appends candidates in canonical order.
+int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
+                     const unsigned *bitmap_l, const Draws &d, int loops_thresh, unsigned epoch,
+                     unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
+                     cudaStream_t st);
+int vote_launches_per_loop();
+
+// A8: estimates + |value|^2 keys for the candidates.
+int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, const void *bins,
+                    int loops, int n, int B, const Draws &d, const double2 *hinv,
+                    DevNode *nodes, double *mag2, cudaStream_t st);
+
+// gather selected nodes (A9 output)
+int launch_gather_nodes(const DevNode *nodes, const int *idx, const int *count, int cap,
+                        DevNode *out, cudaStream_t st);
+
+}  // namespace gsfft

@@ -1,0 +1,251 @@
+"""Host-side Python binding of libgsfft.so (include/gsfft.h) via ctypes.
+
+This mirrors the reference's host interface for the sparse-FFT path
+(outerLoop.h:35-38, innerLoop.h:32-50) plus the native plan API.  Device
+buffers are passed as raw pointers (e.g. ``torch.Tensor.data_ptr()``); streams
+as ``torch.cuda.Stream.cuda_stream`` integers (0 = default stream).
+
+The CUDA library is required: every entry raises if libgsfft.so is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "build", "libgsfft.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "gsfft.h")
+
+FP64, MIXED = 0, 1
+FLAG_QUIRK_RESIDUE = 1
+OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE = range(7)
+
+NODE = np.dtype({"names": ["key", "x", "y"], "formats": ["<u4", "<f8", "<f8"],
+                 "offsets": [0, 8, 16], "itemsize": 24})
+
+
+class GsfftError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__(f"{what}: status {status} ({status_string(status)}) {last_error()}")
+
+
+class Params(C.Structure):
+    _fields_ = [(f, C.c_int) for f in (
+        "q", "n", "k", "B", "B_thresh", "W_RLFC", "RLFC_loops", "loops_loc",
+        "loops_thresh", "loops_est", "loops", "b_f", "w")] + [
+        (f, C.c_double) for f in ("Bcst", "RLFC_cst", "BB", "lobefrac", "tolerance", "t0")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def build():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gsfft_build_lib", os.path.join(PKG, "build_lib.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m.build()
+
+
+def lib():
+    """Loads libgsfft.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libgsfft.so not built ({LIB_PATH}); run gpu-sfft_gb300/build_lib.py")
+    L = C.CDLL(LIB_PATH)
+    P, i, d, u = C.c_void_p, C.c_int, C.c_double, C.c_uint
+    ll = C.c_longlong
+    sig = {
+        "gsfft_version": ([], C.c_char_p),
+        "gsfft_last_error": ([], C.c_char_p),
+        "gsfft_status_string": ([i], C.c_char_p),
+        "gsfft_derive_params": ([i, i, d, i, i, i, d, i, d, C.POINTER(Params)], i),
+        "gsfft_design_filter": ([C.POINTER(Params), P, P, P], i),
+        "gsfft_plan_create": ([C.POINTER(Params), i, u, i, C.POINTER(P)], i),
+        "gsfft_plan_destroy": ([P], i),
+        "gsfft_plan_set_filter": ([P, P, P, P], i),
+        "gsfft_run": ([P, P, P, P, P, P], i),
+        "gsfft_get_results": ([P, P, i, C.POINTER(i), P, i, C.POINTER(i), P], i),
+        "gsfft_device_results": ([P, P, P, P, P], i),
+        "gsfft_debug_stages": ([P, P, C.POINTER(i), P, P, P], i),
+        "gsfft_plan_launches_per_run": ([P], i),
+        "gsfft_plan_enable_timing": ([P, i], i),
+        "gsfft_plan_stage_times": ([P, C.POINTER(C.c_float), i, C.POINTER(i)], i),
+        "gsfft_stage_name": ([i], C.c_char_p),
+        "gsfft_fft": ([P, P, ll, i, i, i, P], i),
+        "gsfft_cutoff": ([P, i, i, i, i, P, P], i),
+        "gsfft_stage_perm_filter": ([i, P, i, P, i, i, i, P, i, P, P], i),
+        "gsfft_stage_reverse_hash": ([P, i, P, i, i, i, i, i, i, i, u, P, P, i,
+                                      C.POINTER(i), P], i),
+        "gsfft_stage_estimate": ([i, P, i, P, i, i, i, P, P, P, P], i),
+        "outer_loop": ([P, i, P, P, i, i, i, i, i, i, i, i, C.POINTER(i), C.c_float], P),
+        "timesmod": ([i, i, i], i),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def version():
+    return lib().gsfft_version().decode()
+
+
+def last_error():
+    return lib().gsfft_last_error().decode(errors="replace")
+
+
+def status_string(s):
+    return lib().gsfft_status_string(s).decode()
+
+
+def check(status, what):
+    if status != OK:
+        raise GsfftError(status, what)
+
+
+def exported_header_symbols():
+    """Function names declared in include/gsfft.h."""
+    import re
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w \*]*?\b(\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "defined")))
+
+
+def derive_params(q, k, Bcst, loops_loc, loops_thresh, loops_est, RLFC_cst, RLFC_loops,
+                  tolerance=1e-8):
+    p = Params()
+    s = lib().gsfft_derive_params(q, k, Bcst, loops_loc, loops_thresh, loops_est, float(RLFC_cst),
+                                  RLFC_loops, tolerance, C.byref(p))
+    return p, s
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def design_filter(p, d_filter_time, d_filter_freq=0, stream=0):
+    check(lib().gsfft_design_filter(C.byref(p), d_filter_time, d_filter_freq or None, stream or None),
+          "gsfft_design_filter")
+
+
+def fft(d_in, d_out, n, batch=1, sign=-1, precision=FP64, stream=0):
+    check(lib().gsfft_fft(d_in, d_out, n, batch, sign, precision, stream or None), "gsfft_fft")
+
+
+def cutoff(d_samples, size, num, batch, precision, d_out, stream=0):
+    check(lib().gsfft_cutoff(d_samples, size, num, batch, precision, d_out, stream or None),
+          "gsfft_cutoff")
+
+
+def stage_perm_filter(precision, d_x, n, d_filter_time, w, B, ai, d_bins, quirk_residue=False,
+                      stream=0):
+    ai = np.ascontiguousarray(ai, np.int32)
+    check(lib().gsfft_stage_perm_filter(precision, d_x, n, d_filter_time, w, B, ai.size,
+                                        _np_ptr(ai), int(quirk_residue), d_bins, stream or None),
+          "gsfft_stage_perm_filter")
+
+
+def stage_reverse_hash(d_J, B_thresh, d_J2, num_RLFC, n, B, W, a, ai, loops_thresh, epoch,
+                       d_vote, d_cand, cap, count, stream=0):
+    c = C.c_int(count)
+    s = lib().gsfft_stage_reverse_hash(d_J, B_thresh, d_J2, num_RLFC, n, B, W, a, ai, loops_thresh,
+                                       epoch, d_vote, d_cand, cap, C.byref(c), stream or None)
+    return s, c.value
+
+
+def stage_estimate(precision, d_cand, num, d_bins, loops, n, B, ai, d_filter_freq, d_out,
+                   stream=0):
+    ai = np.ascontiguousarray(ai, np.int32)
+    check(lib().gsfft_stage_estimate(precision, d_cand, num, d_bins, loops, n, B, _np_ptr(ai),
+                                     d_filter_freq, d_out, stream or None), "gsfft_stage_estimate")
+
+
+class Plan:
+    """One reusable sparse-FFT plan (all device buffers allocated here)."""
+
+    def __init__(self, params, precision=FP64, flags=0, max_candidates=0):
+        self.params = params
+        self.precision = precision
+        h = C.c_void_p()
+        check(lib().gsfft_plan_create(C.byref(params), precision, flags, max_candidates,
+                                      C.byref(h)), "gsfft_plan_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().gsfft_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_filter(self, d_filter_time, d_filter_freq, stream=0):
+        check(lib().gsfft_plan_set_filter(self.h, d_filter_time, d_filter_freq, stream or None),
+              "gsfft_plan_set_filter")
+
+    def run(self, d_x, offsets, a, ai, stream=0):
+        self._draws = [np.ascontiguousarray(v, np.int32) for v in (offsets, a, ai)]
+        o, aa, ii = self._draws
+        check(lib().gsfft_run(self.h, d_x, _np_ptr(o), _np_ptr(aa), _np_ptr(ii), stream or None),
+              "gsfft_run")
+
+    def results(self, stream=0, cap=None):
+        I_F = C.c_int(0)
+        ntop = C.c_int(0)
+        s = lib().gsfft_get_results(self.h, None, 0, C.byref(I_F), None, 0, C.byref(ntop),
+                                    stream or None)
+        if s not in (OK, ERR_CAPACITY):
+            check(s, "gsfft_get_results")
+        m = I_F.value if cap is None else min(cap, I_F.value)
+        nodes = np.zeros(max(m, 1), NODE)
+        top = np.zeros(max(ntop.value, 1), NODE)
+        s = lib().gsfft_get_results(self.h, _np_ptr(nodes), m, C.byref(I_F), _np_ptr(top),
+                                    ntop.value, C.byref(ntop), stream or None)
+        return {"status": s, "I_F": I_F.value, "nodes": nodes[:min(m, I_F.value)],
+                "topk": top[:ntop.value]}
+
+    def debug_stages(self, stream=0):
+        p = self.params
+        J2 = np.zeros(p.RLFC_loops * p.B_thresh, np.int32)
+        J = np.zeros(p.loops_loc * p.B_thresh, np.int32)
+        bins = np.zeros(p.loops * p.B, np.complex128 if self.precision == FP64 else np.complex64)
+        nr = C.c_int(0)
+        check(lib().gsfft_debug_stages(self.h, _np_ptr(J2), C.byref(nr), _np_ptr(J),
+                                       _np_ptr(bins), stream or None), "gsfft_debug_stages")
+        return {"J2": J2[:nr.value], "J": J.reshape(p.loops_loc, p.B_thresh),
+                "bins": bins.reshape(p.loops, p.B)}
+
+    def enable_timing(self, on=True):
+        check(lib().gsfft_plan_enable_timing(self.h, int(on)), "gsfft_plan_enable_timing")
+
+    def stage_times(self):
+        """{stage name: average ms} over the runs since the last call."""
+        ms = (C.c_float * 16)()
+        runs = C.c_int(0)
+        check(lib().gsfft_plan_stage_times(self.h, ms, 16, C.byref(runs)), "gsfft_plan_stage_times")
+        out = {}
+        for i in range(16):
+            name = lib().gsfft_stage_name(i).decode()
+            if not name:
+                break
+            out[name] = ms[i]
+        return out, runs.value
+
+    def launches_per_run(self):
+        return lib().gsfft_plan_launches_per_run(self.h)

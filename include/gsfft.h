@@ -1,0 +1,206 @@
+/*
+ * gsfft.h -- C ABI of the GB300 (sm_103a) sparse-FFT engine.
+ *
+ * Two layers:
+ *   1. Drop-in entry points with the reference's exact names and signatures
+ *      (pcdslab/gpu-sfft outerLoop.h:35-38, innerLoop.h:32-50).  A C program
+ *      written against the reference links against libgsfft.so unchanged.
+ *   2. The native gsfft_* API: explicit plans, status codes instead of exit(),
+ *      caller-chosen CUDA stream, random draws passed in by the caller, FP64 or
+ *      mixed (FP32 signal/buckets, FP64 estimate) precision.
+ *
+ * All pointers named d_* are device pointers (managed memory also works).
+ * Every gsfft_* call returns a gsfft_status; none of them exits the process.
+ */
+#ifndef GSFFT_H_
+#define GSFFT_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#define GSFFT_VERSION_STRING "0.1.0"
+
+/* ---- types shared with the reference (utils.h:32-51) ------------------- */
+#ifndef GSFFT_NO_REFERENCE_TYPES
+/* complex_t: same layout as cufftDoubleComplex (utils.h:32-35). */
+typedef struct double2C { double x; double y; } complex_t;
+/* Node: 4-byte key, 4 bytes padding, 16-byte value (utils.h:42-45). */
+typedef struct nodes { unsigned int key; complex_t value; } Node;
+/* Pair (utils.h:48-51). */
+typedef struct pairs { int first; int second; } Pair;
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+typedef enum {
+  GSFFT_OK = 0,
+  GSFFT_ERR_PARAM = 1,       /* a parameter violates a reference assert or a limit */
+  GSFFT_ERR_CAPACITY = 2,    /* candidate list larger than the plan's capacity */
+  GSFFT_ERR_ALLOC = 3,       /* device or host allocation failed */
+  GSFFT_ERR_CUDA = 4,        /* a CUDA runtime call failed (see gsfft_last_error) */
+  GSFFT_ERR_UNSUPPORTED = 5, /* size or mode outside what this build supports */
+  GSFFT_ERR_STATE = 6        /* plan used before gsfft_plan_set_filter, or similar */
+} gsfft_status;
+
+typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
+
+/* Plan flags. */
+#define GSFFT_FLAG_QUIRK_RESIDUE 1u  /* reproduce permFilterTillKernel's residue
+                                        tap index (innerLoop.cu:745-754) */
+
+/* Run parameters derived exactly as experiment.c:71-84 and
+ * cuExperiment.cu:279-284 derive them. */
+typedef struct {
+  int q, n, k;
+  int B, B_thresh, W_RLFC, RLFC_loops;
+  int loops_loc, loops_thresh, loops_est, loops;
+  int b_f, w;
+  double Bcst, RLFC_cst, BB, lobefrac, tolerance, t0;
+} gsfft_params;
+
+/* Replaces experiment.c:54-84 (+ the filter-size computation of
+ * cuExperiment.cu:279-284).  Returns GSFFT_ERR_PARAM where the reference
+ * would fail an assert (experiment.c:77,82-84; cuExperiment.cu:283) and for
+ * the degenerate window layouts this engine rejects (W_RLFC >= n,
+ * W_RLFC <= n/B). */
+int gsfft_derive_params(int q, int k, double Bcst, int loops_loc, int loops_thresh,
+                        int loops_est, double RLFC_cst, int RLFC_loops,
+                        double tolerance, gsfft_params *out);
+
+/* Replaces the filter part of make_multiple_t (filters.h:44-48,
+ * cuExperiment.cu:277-448), entirely on the GPU in FP64.
+ * d_filter_time: p->w taps; d_filter_freq: p->n bins (may be NULL).
+ * Allocates its own scratch (about 3 * n * 16 bytes) for the call. */
+int gsfft_design_filter(const gsfft_params *p, complex_t *d_filter_time,
+                        complex_t *d_filter_freq, void *stream);
+
+/* ---- plans ------------------------------------------------------------- */
+typedef struct gsfft_plan_s *gsfft_plan;
+
+/* Allocates every buffer the pipeline needs once (no allocation in
+ * gsfft_run).  max_candidates <= 0 selects the reference's MAXSIZE_HITS
+ * (utils.h:40, 524288). */
+int gsfft_plan_create(const gsfft_params *p, int precision, unsigned flags,
+                      int max_candidates, gsfft_plan *out);
+int gsfft_plan_destroy(gsfft_plan plan);
+
+/* Installs the filter: w time taps and the full n-bin response (only the
+ * n/B bins around 0 that the estimate reads are kept). */
+int gsfft_plan_set_filter(gsfft_plan plan, const complex_t *d_filter_time,
+                          const complex_t *d_filter_freq, void *stream);
+
+/* One sparse FFT (the outer_loop of outerLoop.cu:65-190) on stream.
+ * d_x: n complex samples, complex_t (FP64) or {float x, y} (MIXED).
+ * h_rlfc_offsets[RLFC_loops], h_a[loops], h_ai[loops]: the random draws of
+ * innerLoop.cu:123 and outerLoop.cu:128-134 (ai = a^-1 mod n).
+ * Asynchronous: results stay on the device until gsfft_get_results. */
+int gsfft_run(gsfft_plan plan, const void *d_x, const int *h_rlfc_offsets,
+              const int *h_a, const int *h_ai, void *stream);
+
+/* Synchronises stream and copies the results to host memory:
+ * all candidates (I_F Nodes, canonical order) and the k largest by |value|
+ * (A9 of the evaluation, cuExperiment.cu:184-193).  Either output may be NULL.
+ * Returns GSFFT_ERR_CAPACITY when the candidate list overflowed. */
+int gsfft_get_results(gsfft_plan plan, Node *h_nodes, int nodes_cap, int *I_F,
+                      Node *h_topk, int topk_cap, int *n_topk, void *stream);
+
+/* Device-side views of the last run's results (valid until the next run). */
+int gsfft_device_results(gsfft_plan plan, const Node **d_nodes, const int **d_I_F,
+                         const Node **d_topk, const int **d_n_topk);
+
+/* Intermediate stage outputs of the last run, copied to host (for checking):
+ * J2 (num_RLFC ids), J (loops_loc * B_thresh ids), bins (loops * B complex,
+ * complex_t in FP64, {float,float} in MIXED).  Any pointer may be NULL. */
+int gsfft_debug_stages(gsfft_plan plan, int *h_J2, int *num_RLFC, int *h_J,
+                       void *h_bins, void *stream);
+
+/* Per-stage CUDA-event timing of gsfft_run (off by default).  Stages, in
+ * order: rlfc_fft, rlfc_select, j2_merge, perm_filter, bucket_fft, cutoff,
+ * vote, estimate, topk.  gsfft_plan_stage_times synchronises the device,
+ * returns the average ms per stage over the runs since the last call and
+ * restarts the average. */
+int gsfft_plan_enable_timing(gsfft_plan plan, int on);
+int gsfft_plan_stage_times(gsfft_plan plan, float *ms_avg, int max_stages, int *runs);
+const char *gsfft_stage_name(int stage);
+
+/* Number of kernel launches one gsfft_run issues for this plan. */
+int gsfft_plan_launches_per_run(gsfft_plan plan);
+
+/* ---- building blocks (also used by the stage drop-ins) ------------------ */
+
+/* Batched unnormalised complex FFT of power-of-two size n_fft >= 256,
+ * out-of-place or in place; sign -1 forward, +1 inverse; precision selects
+ * complex_t or {float, float} elements. */
+int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
+              int precision, void *stream);
+
+/* Cutoff (innerLoop.cu:551-616): indices of the num largest samples, ascending;
+ * ties at the threshold resolved in ascending index order.  batch independent
+ * rows of `size` samples each (double or float per precision). */
+int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precision,
+                 int *d_out, void *stream);
+
+/* Stage entry points (one stage of the pipeline on caller buffers).
+ * A5 (perm_filter_cutoff's first half, innerLoop.cu:194-240): bins[l*B + b]
+ * for l < loops, before the bucket FFT.  d_x / d_bins hold complex_t (FP64)
+ * or {float, float} (MIXED); the taps are given as complex_t. */
+int gsfft_stage_perm_filter(int precision, const void *d_x, int n,
+                            const complex_t *d_filter_time, int w, int B, int loops,
+                            const int *h_ai, int quirk_residue, void *d_bins, void *stream);
+/* A7 (reverse_hash, innerLoop.cu:300-384) for one location loop.  d_vote: n
+ * entries, epoch << 8 | count (epoch 0 = plain counts, the reference's int
+ * table).  Appends to d_cand from *h_count on; *h_count is updated (it may
+ * exceed cap, in which case GSFFT_ERR_CAPACITY is returned). */
+int gsfft_stage_reverse_hash(const int *d_J, int B_thresh, const int *d_J2, int num_RLFC,
+                             int n, int B, int W_RLFC, int a, int ai, int loops_thresh,
+                             unsigned epoch, unsigned *d_vote, int *d_cand, int cap,
+                             int *h_count, void *stream);
+/* A8 (estimate_values, innerLoop.cu:396-466): d_out[i] for i < num. */
+int gsfft_stage_estimate(int precision, const int *d_cand, int num, const void *d_bins,
+                         int loops, int n, int B, const int *h_ai,
+                         const complex_t *d_filter_freq, Node *d_out, void *stream);
+
+/* ---- drop-in entry points with the reference's signatures -------------- */
+
+/* outerLoop.h:35-38.  Draws the RLFC offsets with drand48() and the
+ * permutations with random() in the reference's order, runs the FP64 engine
+ * (residue quirk on for n < 2^27, like the reference's kernel switch at
+ * innerLoop.cu:230) and returns a malloc'ed host array of *I_F Nodes
+ * (caller frees).  d_filter_size is the tap count w.  Returns NULL on error
+ * (message in gsfft_last_error). */
+Node *outer_loop(complex_t *d_x, int n, complex_t *d_filter_time,
+                 complex_t *d_filter_freq, int d_filter_size, int B, int B_thresh,
+                 int W_RLFC, int RLFC_loops, int loop_threshold, int loops_loc,
+                 int loops, int *I_F, float t_H_to_D);
+
+/* innerLoop.h:32-50.  Same arguments and effects as the reference; the timing
+ * accumulators are advanced by the CUDA-event time of the call. */
+int restr_loc_freq_coeff(complex_t *d_x, int n, int B_thresh, int W_RLFC, int *d_J2,
+                         double *RLFC_Time);
+int samples_indices(complex_t *d_samp, int B, int samp_size, int *d_output,
+                    double *CTime);
+int perm_filter_cutoff(complex_t *d_x, int n, complex_t *d_filter_time,
+                       int d_filter_size, int B_thresh, int B, int a, int ai,
+                       complex_t *d_bins_f, int *d_J, double *PF_T, double *BC_T);
+int reverse_hash(int *d_J, int n, int B_thresh, int B, int a, int ai, int loop_thresh,
+                 int *d_vote, int *d_I, int *I_F, double *G_T, int *d_J2,
+                 int num_RLFC, int W_RLFC, int RLFC_loops);
+Node *estimate_values(int *d_I, int *I_F, complex_t *d_bins_f, int loops, int n,
+                      int *permute, int B, complex_t *d_filter_freq, int loops_loc);
+int timesmod(const int x, const int a, const int n);
+
+/* ---- misc -------------------------------------------------------------- */
+const char *gsfft_version(void);
+const char *gsfft_last_error(void);
+const char *gsfft_status_string(int status);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif /* GSFFT_H_ */

@@ -1,0 +1,61 @@
+"""CPU-side checks of the C ABI: the library loads, exports every function
+declared in include/gsfft.h, and its host-only entry points (parameter
+derivation, version, status strings) behave.  No GPU calls."""
+import ctypes as C
+
+import pytest
+
+
+def test_exports_every_declared_symbol(G):
+    declared = G.exported_header_symbols()
+    assert "outer_loop" in declared and "gsfft_run" in declared
+    L = G.lib()
+    missing = [s for s in declared if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_reference_dropin_symbols(G):
+    # innerLoop.h:32-50 / outerLoop.h:35-38 names the reference's callers bind
+    for s in ("outer_loop", "timesmod"):
+        assert hasattr(G.lib(), s)
+
+
+def test_version_and_status(G):
+    assert G.version() == "0.1.0"
+    assert G.status_string(0) == "ok"
+    assert "capacity" in G.status_string(G.ERR_CAPACITY)
+
+
+@pytest.mark.parametrize("args", [
+    (27, 16000, 0.65, 2, 2, 7, 4096, 2),
+    (20, 1000, 1.40, 2, 2, 5, 128, 2),
+    (27, 43000, 0.8, 3, 2, 8, 32768, 2),
+    (18, 100, 1.0, 3, 2, 6, 32, 2),
+])
+def test_derive_params_matches_oracle(G, O, args):
+    pg, sg = G.derive_params(*args)
+    po, so = O.derive_params(*args)
+    assert sg == so == 0
+    assert pg.as_dict() == po.as_dict()
+
+
+def test_derive_params_rejects(G):
+    _, s = G.derive_params(18, 4000, 1.0, 2, 2, 5, 128, 2)   # B_thresh >= B
+    assert s == G.ERR_PARAM
+    _, s = G.derive_params(20, 1000, 1.4, 1, 2, 5, 128, 2)   # loops_thresh > loops_loc
+    assert s == G.ERR_PARAM
+    _, s = G.derive_params(20, 1000, 1.4, 2, 2, 5, 0.001, 2)  # W_RLFC < 2 k
+    assert s != 0
+
+
+def test_timesmod(G):
+    assert G.lib().timesmod(123456789, 987654321 % (1 << 30), 1 << 27) == \
+        (123456789 * (987654321 % (1 << 30))) % (1 << 27)
+
+
+def test_null_arguments_rejected(G):
+    L = G.lib()
+    assert L.gsfft_run(None, None, None, None, None, None) == G.ERR_PARAM
+    assert L.gsfft_plan_destroy(None) == G.ERR_PARAM
+    p = G.Params()
+    assert L.gsfft_plan_create(C.byref(p), 0, 0, 0, None) == G.ERR_PARAM

@@ -1,0 +1,186 @@
+"""End-to-end parity of the GPU engine (through the C ABI) with the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gsfft import synth
+
+pytestmark = pytest.mark.gpu
+
+CFGS = {  # (q, k, Bcst, loops_loc, loops_thresh, loops_est, RLFC_cst, RLFC_loops)
+    "n14": (14, 10, 2.5, 2, 2, 5, 16, 2),
+    "n16": (16, 20, 1.0, 2, 2, 5, 8, 2),
+    "n18_3loc": (18, 100, 1.0, 3, 2, 6, 32, 2),
+    "config1": (20, 1000, 1.40, 2, 2, 5, 128, 2),
+}
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def setup(G, O, torch, cfg, seed=0, snr_db=None):
+    p_o, st = O.derive_params(*cfg)
+    assert st == 0
+    p_g, st = G.derive_params(*cfg)
+    assert st == 0
+    assert p_g.as_dict() == p_o.as_dict()
+    x, loc, coef, X = synth.signal_numpy(p_o.n, p_o.k, seed=seed, snr_db=snr_db)
+    ft, ff = O.design_filter(p_o)
+    draws = synth.draws(seed, p_o.n, p_o.W_RLFC, p_o.RLFC_loops, p_o.loops)
+    return p_o, p_g, x, loc, X, ft, ff, draws
+
+
+def run_gpu(G, torch, p_g, x, ft, ff, draws, prec=0, flags=0):
+    plan = G.Plan(p_g, prec, flags)
+    d_ft, d_ff = dev(torch, ft), dev(torch, ff)
+    plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+    d_x = dev(torch, x.astype(np.complex128 if prec == 0 else np.complex64))
+    plan.run(d_x.data_ptr(), *draws)
+    res = plan.results()
+    res["stages"] = plan.debug_stages()
+    res["launches"] = plan.launches_per_run()
+    plan.close()
+    return res
+
+
+@pytest.mark.parametrize("name", list(CFGS))
+def test_fp64_pipeline_vs_oracle(G, O, torch_cuda, name):
+    torch = torch_cuda
+    cfg = CFGS[name]
+    p, p_g, x, loc, X, ft, ff, (offs, a, ai) = setup(G, O, torch, cfg)
+    g = run_gpu(G, torch, p_g, x, ft, ff, (offs, a, ai))
+    assert g["status"] == 0
+    o = O.outer_loop(x, p, ft, ff, offs, a, ai, want_stages=True)
+    st = g["stages"]
+    # J2: every significant RLFC bin is selected on both sides; picks among
+    # bins at FFT rounding level (noiseless signal) may differ.
+    spec_sig = set()
+    for r in range(p.RLFC_loops):
+        _, yf = O.rlfc(x, p.n, p.W_RLFC, p.B_thresh, int(offs[r]), want_spectrum=True)
+        mag = np.abs(yf) ** 2
+        spec_sig |= set(np.nonzero(mag > 1e-12 * mag.max())[0].tolist())
+    j2_g = set(st["J2"].tolist())
+    j2_o = set(O.merge_j2(list(o["J2_blocks"])).tolist())
+    assert spec_sig <= j2_g and spec_sig <= j2_o
+    # bucket spectra: FP64 FFT parity
+    bins_o = o["bins_f"]
+    assert np.abs(st["bins"] - bins_o).max() <= 1e-11 * np.abs(bins_o).max()
+    # stage injection: the oracle's cutoff on the GPU's bins gives the GPU's J
+    for l in range(p.loops_loc):
+        np.testing.assert_array_equal(st["J"][l], O.cutoff(O.samples(st["bins"][l]), p.B_thresh))
+    # stage injection: the oracle's vote on the GPU's J and J2 gives the GPU's
+    # candidates in the same (canonical) order
+    vote = np.zeros(p.n, np.int32)
+    cand = []
+    for l in range(p.loops_loc):
+        c, vote, s = O.reverse_hash(st["J"][l], st["J2"], p.n, p.B, p.W_RLFC, int(a[l]), int(ai[l]),
+                                    p.loops_thresh, vote=vote, cand=cand)
+        cand = list(c)
+    np.testing.assert_array_equal(g["nodes"]["key"], np.array(cand, np.uint32))
+    est = O.estimate(np.array(cand, np.int32), st["bins"], p.loops, p.n, ai, p.B, ff)
+    scale = max(1.0, np.abs(est["x"] + 1j * est["y"]).max())
+    assert np.abs(g["nodes"]["x"] - est["x"]).max() <= 1e-12 * scale
+    assert np.abs(g["nodes"]["y"] - est["y"]).max() <= 1e-12 * scale
+    # end to end: the recovered (top-k) location set is identical, values 1e-9
+    top_o = O.topk(o["nodes"], p.k)
+    top_g = g["topk"]
+    assert set(top_g["key"].tolist()) == set(top_o["key"].tolist())
+    vo = dict(zip(top_o["key"].tolist(), top_o["x"] + 1j * top_o["y"]))
+    vg = np.array([vo[k] for k in top_g["key"].tolist()])
+    got = top_g["x"] + 1j * top_g["y"]
+    assert np.abs(got - vg).max() <= 1e-9 * np.abs(vg).max()
+
+
+@pytest.mark.parametrize("name", ["n16", "config1"])
+def test_fp64_residue_quirk(G, O, torch_cuda, name):
+    """GSFFT_FLAG_QUIRK_RESIDUE reproduces permFilterTillKernel's tap indexing."""
+    torch = torch_cuda
+    p, p_g, x, loc, X, ft, ff, (offs, a, ai) = setup(G, O, torch, CFGS[name], seed=3)
+    g = run_gpu(G, torch, p_g, x, ft, ff, (offs, a, ai), flags=G.FLAG_QUIRK_RESIDUE)
+    o = O.outer_loop(x, p, ft, ff, offs, a, ai, quirks=O.QUIRK_RESIDUE, want_stages=True)
+    assert np.abs(g["stages"]["bins"] - o["bins_f"]).max() <= 1e-11 * np.abs(o["bins_f"]).max()
+    assert set(g["topk"]["key"].tolist()) == set(O.topk(o["nodes"], p.k)["key"].tolist())
+
+
+def test_deterministic_repeat(G, O, torch_cuda):
+    torch = torch_cuda
+    p, p_g, x, loc, X, ft, ff, draws = setup(G, O, torch, CFGS["config1"], seed=5)
+    plan = G.Plan(p_g, 0)
+    d_ft, d_ff, d_x = dev(torch, ft), dev(torch, ff), dev(torch, x)
+    plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+    outs = []
+    for _ in range(3):
+        plan.run(d_x.data_ptr(), *draws)
+        outs.append(plan.results())
+    for r in outs[1:]:
+        assert r["nodes"].tobytes() == outs[0]["nodes"].tobytes()
+        assert r["topk"].tobytes() == outs[0]["topk"].tobytes()
+    plan.close()
+
+
+@pytest.mark.parametrize("name,snr", [("n18_3loc", None), ("config1", None), ("config1", 40.0)])
+def test_mixed_vs_fp64(G, O, torch_cuda, name, snr):
+    """Mixed path: same recovered location set as FP64, value rel-L2 <= 1e-5."""
+    torch = torch_cuda
+    p, p_g, x, loc, X, ft, ff, draws = setup(G, O, torch, CFGS[name], seed=7, snr_db=snr)
+    g64 = run_gpu(G, torch, p_g, x, ft, ff, draws, prec=0)
+    g32 = run_gpu(G, torch, p_g, x, ft, ff, draws, prec=1)
+    k64 = g64["topk"]["key"].tolist()
+    assert set(g32["topk"]["key"].tolist()) == set(k64)
+    v64 = dict(zip(k64, g64["topk"]["x"] + 1j * g64["topk"]["y"]))
+    v32 = np.array([complex(r["x"], r["y"]) for r in g32["topk"]])
+    ref = np.array([v64[k] for k in g32["topk"]["key"].tolist()])
+    rel = np.linalg.norm(v32 - ref) / np.linalg.norm(ref)
+    assert rel <= 1e-5, rel
+
+
+def test_outer_loop_dropin(G, O, torch_cuda):
+    """The reference-signature outer_loop (outerLoop.h:35-38) with glibc draws."""
+    torch = torch_cuda
+    cfg = CFGS["config1"]
+    p, p_g, x, loc, X, ft, ff, _ = setup(G, O, torch, cfg, seed=9)
+    offs, a, ai = O.draw_glibc(1234, p.n, p.W_RLFC, p.RLFC_loops, p.loops)
+    O.lib().srand48(1234)
+    O.lib().srandom(1234)
+    d_x, d_ft, d_ff = dev(torch, x), dev(torch, ft), dev(torch, ff)
+    I_F = C.c_int(0)
+    ptr = G.lib().outer_loop(d_x.data_ptr(), p.n, d_ft.data_ptr(), d_ff.data_ptr(), p.w, p.B,
+                             p.B_thresh, p.W_RLFC, p.RLFC_loops, p.loops_thresh, p.loops_loc,
+                             p.loops, C.byref(I_F), C.c_float(0.0))
+    assert ptr, G.last_error()
+    nodes = np.ctypeslib.as_array((C.c_char * (24 * I_F.value)).from_address(ptr)).view(G.NODE).copy()
+    C.CDLL(None).free(C.c_void_p(ptr))
+    o = O.outer_loop(x, p, ft, ff, offs, a, ai, quirks=O.QUIRK_RESIDUE)
+    top_o = O.topk(o["nodes"], p.k)
+    top_g = O.topk(nodes, p.k)
+    assert set(top_g["key"].tolist()) == set(top_o["key"].tolist())
+
+
+def test_filter_design_gpu(G, O, torch_cuda):
+    torch = torch_cuda
+    cfg = CFGS["n18_3loc"]
+    p_o, _ = O.derive_params(*cfg)
+    p_g, _ = G.derive_params(*cfg)
+    ft_o, ff_o = O.design_filter(p_o)
+    d_ft = torch.zeros(p_g.w, dtype=torch.complex128, device="cuda")
+    d_ff = torch.zeros(p_g.n, dtype=torch.complex128, device="cuda")
+    G.design_filter(p_g, d_ft.data_ptr(), d_ff.data_ptr())
+    ft, ff = d_ft.cpu().numpy(), d_ff.cpu().numpy()
+    assert np.abs(ff - ff_o).max() <= 1e-10
+    assert np.abs(ft - ft_o).max() <= 1e-10 * np.abs(ft_o).max()
+
+
+def test_plan_rejects_bad_draws(G, O, torch_cuda):
+    torch = torch_cuda
+    p, p_g, x, loc, X, ft, ff, (offs, a, ai) = setup(G, O, torch, CFGS["n16"])
+    plan = G.Plan(p_g, 0)
+    with pytest.raises(G.GsfftError):  # run before the filter is installed
+        plan.run(dev(torch, x).data_ptr(), offs, a, ai)
+    plan.set_filter(dev(torch, ft).data_ptr(), dev(torch, ff).data_ptr())
+    bad = a.copy()
+    bad[0] = 2  # even: not invertible mod 2^q
+    with pytest.raises(G.GsfftError):
+        plan.run(dev(torch, x).data_ptr(), offs, bad, ai)
+    plan.close()

@@ -1,0 +1,157 @@
+"""GPU parity of each stage against the oracle, through the C ABI.
+
+Index work (cutoff, J2, voting, candidates) must be bit-exact; FP64 numeric
+stages are held to the tolerances written in each test."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("n,batch", [(256, 3), (4096, 2), (8192, 1), (1 << 14, 2), (1 << 17, 3),
+                                     (1 << 20, 1), (1 << 22, 2), (1 << 25, 1)])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_fft_vs_numpy(G, torch_cuda, n, batch, prec):
+    torch = torch_cuda
+    rng = np.random.default_rng(n + batch)
+    x = (rng.normal(size=(batch, n)) + 1j * rng.normal(size=(batch, n)))
+    ref = np.fft.fft(x, axis=1)
+    refi = np.fft.ifft(x, axis=1) * n
+    dt = np.complex128 if prec == 0 else np.complex64
+    tol = 1e-13 if prec == 0 else 3e-6
+    d_in = dev(torch, x.astype(dt))
+    d_out = torch.empty_like(d_in)
+    G.fft(d_in.data_ptr(), d_out.data_ptr(), n, batch, -1, prec)
+    got = d_out.cpu().numpy()
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= tol * scale * np.log2(n)
+    G.fft(d_in.data_ptr(), d_out.data_ptr(), n, batch, +1, prec)
+    got = d_out.cpu().numpy()
+    assert np.abs(got - refi).max() <= tol * scale * np.log2(n)
+    # in place
+    G.fft(d_in.data_ptr(), d_in.data_ptr(), n, batch, -1, prec)
+    assert np.abs(d_in.cpu().numpy() - ref).max() <= tol * scale * np.log2(n)
+
+
+@pytest.mark.parametrize("size,num,batch", [(300, 7, 1), (5000, 2000, 2), (131072, 32000, 2),
+                                            (70001, 3, 1), (1 << 20, 4000, 2)])
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("ties", [False, True])
+def test_cutoff_exact(G, O, torch_cuda, size, num, batch, prec, ties):
+    torch = torch_cuda
+    rng = np.random.default_rng(size + num)
+    if ties:
+        s = rng.integers(0, 9, size=(batch, size)).astype(np.float64) ** 2
+    else:
+        s = np.abs(rng.normal(size=(batch, size))) ** 3
+    s = s.astype(np.float64 if prec == 0 else np.float32)
+    d_s = dev(torch, s)
+    d_out = torch.zeros((batch, num), dtype=torch.int32, device="cuda")
+    G.cutoff(d_s.data_ptr(), size, num, batch, prec, d_out.data_ptr())
+    got = d_out.cpu().numpy()
+    for b in range(batch):
+        np.testing.assert_array_equal(got[b], O.cutoff(s[b], num))
+
+
+@pytest.mark.parametrize("quirk", [False, True])
+def test_perm_filter_bitexact_fp64(G, O, torch_cuda, quirk):
+    torch = torch_cuda
+    rng = np.random.default_rng(21)
+    n, B, w = 1 << 16, 256, 3479
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    f = rng.normal(size=w) + 1j * rng.normal(size=w)
+    ai = (rng.integers(0, n // 2, size=9) * 2 + 1).astype(np.int32)
+    d_bins = torch.zeros((9, B), dtype=torch.complex128, device="cuda")
+    G.stage_perm_filter(0, dev(torch, x).data_ptr(), n, dev(torch, f).data_ptr(), w, B, ai,
+                        d_bins.data_ptr(), quirk_residue=quirk)
+    got = d_bins.cpu().numpy()
+    for l in range(9):
+        ref = O.perm_filter(x, n, f, B, int(ai[l]), quirks=1 if quirk else 0)
+        np.testing.assert_array_equal(got[l], ref)  # same fma sequence: bit-exact
+
+
+def test_perm_filter_fp32(G, O, torch_cuda):
+    torch = torch_cuda
+    rng = np.random.default_rng(22)
+    n, B, w = 1 << 16, 512, 5001
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    f = rng.normal(size=w) + 1j * rng.normal(size=w)
+    ai = (rng.integers(0, n // 2, size=3) * 2 + 1).astype(np.int32)
+    d_bins = torch.zeros((3, B), dtype=torch.complex64, device="cuda")
+    G.stage_perm_filter(1, dev(torch, x.astype(np.complex64)).data_ptr(), n,
+                        dev(torch, f).data_ptr(), w, B, ai, d_bins.data_ptr())
+    got = d_bins.cpu().numpy()
+    for l in range(3):
+        ref = O.perm_filter(x, n, f, B, int(ai[l]))
+        assert np.abs(got[l] - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_reverse_hash_exact(G, O, torch_cuda, seed):
+    torch = torch_cuda
+    rng = np.random.default_rng(seed)
+    n, B, W, Bt = 1 << 18, 1024, 8192, 200
+    nj2 = [400, 30, 1000, 5][seed]
+    J2 = np.sort(rng.choice(W, nj2, replace=False)).astype(np.int32)
+    a = (rng.integers(0, n // 2, size=3) * 2 + 1)
+    ai = np.array([pow(int(v), -1, n) for v in a])
+    vote_o = np.zeros(n, np.int32)
+    cand_o = []
+    d_vote = torch.zeros(n, dtype=torch.int32, device="cuda")
+    d_cand = torch.zeros(1 << 16, dtype=torch.int32, device="cuda")
+    count = 0
+    d_J2 = dev(torch, J2)
+    for l in range(3):
+        J = np.sort(rng.choice(B, Bt, replace=False)).astype(np.int32)
+        J[0] = 0
+        J = np.unique(J).astype(np.int32)
+        c, vote_o, st = O.reverse_hash(J, J2, n, B, W, int(a[l]), int(ai[l]), 2, vote=vote_o,
+                                       cand=cand_o)
+        cand_o = list(c)
+        s, count = G.stage_reverse_hash(dev(torch, J).data_ptr(), J.size, d_J2.data_ptr(), J2.size,
+                                        n, B, W, int(a[l]), int(ai[l]), 2, 0, d_vote.data_ptr(),
+                                        d_cand.data_ptr(), 1 << 16, count)
+        assert s == 0
+    np.testing.assert_array_equal(d_cand.cpu().numpy()[:count], np.array(cand_o, np.int32))
+    np.testing.assert_array_equal(d_vote.cpu().numpy(), vote_o)
+
+
+def test_reverse_hash_capacity(G, torch_cuda):
+    torch = torch_cuda
+    n, B, W = 1 << 14, 256, 1024
+    J2 = np.arange(0, W, 2, dtype=np.int32)
+    J = np.arange(0, B, 1, dtype=np.int32)[:200]
+    d_vote = torch.zeros(n, dtype=torch.int32, device="cuda")
+    d_cand = torch.full((64,), -7, dtype=torch.int32, device="cuda")
+    s, count = G.stage_reverse_hash(dev(torch, J).data_ptr(), J.size, dev(torch, J2).data_ptr(),
+                                    J2.size, n, B, W, 3, pow(3, -1, n), 1, 0, d_vote.data_ptr(),
+                                    d_cand.data_ptr(), 32, 0)
+    assert s == G.ERR_CAPACITY and count > 32
+    assert (d_cand.cpu().numpy()[32:] == -7).all()  # nothing written past the capacity
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_estimate(G, O, torch_cuda, prec):
+    torch = torch_cuda
+    rng = np.random.default_rng(31)
+    n, B, loops = 1 << 16, 512, 9
+    bins = rng.normal(size=(loops, B)) + 1j * rng.normal(size=(loops, B))
+    ff = rng.normal(size=n) + 1j * rng.normal(size=n) + 2.0
+    ai = np.array([pow(int(v) * 2 + 1, -1, n) for v in rng.integers(0, n // 2, loops)], np.int32)
+    cand = rng.choice(n, 3000, replace=False).astype(np.int32)
+    if prec == 1:
+        bins = bins.astype(np.complex64).astype(np.complex128)
+    ref = O.estimate(cand, bins, loops, n, ai, B, ff)
+    d_out = torch.zeros(cand.size * 3, dtype=torch.float64, device="cuda")
+    G.stage_estimate(prec, dev(torch, cand).data_ptr(), cand.size,
+                     dev(torch, bins.astype(np.complex128 if prec == 0 else np.complex64)).data_ptr(),
+                     loops, n, B, ai, dev(torch, ff).data_ptr(), d_out.data_ptr())
+    got = d_out.cpu().numpy().view(G.NODE)
+    np.testing.assert_array_equal(got["key"], ref["key"])
+    scale = np.abs(ref["x"] + 1j * ref["y"]).max()
+    assert np.abs(got["x"] - ref["x"]).max() <= 1e-13 * scale
+    assert np.abs(got["y"] - ref["y"]).max() <= 1e-13 * scale
