@@ -265,9 +265,17 @@ def run_ours(args, cfg):
             ms = float(t.item())
         return ms, stages, clocks
 
-    ms64, st64, _ = timed("fp64")
+    if args.only_mixed:
+        ms64, st64 = float("nan"), {}
+    else:
+        ms64, st64, _ = timed("fp64")
     sampler = ClockSampler(local)
     ms32, st32, clocks = timed("mixed", sampler)
+    if args.only_mixed:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "ms_per_step": ms32 / args.steps,
+                              "stage_ms": st32, "launches_per_run": plans["mixed"].launches_per_run()}))
+        return 0
 
     # --- accuracy: same signal and draws through both paths
     acc = {}
@@ -392,10 +400,16 @@ def main():
     ap.add_argument("--impl", default="gsfft", choices=["gsfft", "reference"])
     ap.add_argument("--q", type=int, default=None, help=argparse.SUPPRESS)  # smaller n for local checks
     ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="headline", choices=["headline", "small"],
+                    help="small: n=2^25, k=4000 (same W_RLFC) for profiler captures")
+    ap.add_argument("--only-mixed", action="store_true",
+                    help="time only the mixed path and print its stage times (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     cfg = dict(CFG)
+    if args.workload == "small":
+        cfg.update(q=25, k=4000)
     if args.q is not None:
         cfg.update(q=args.q, k=1000, Bcst=1.40, loops_est=5, RLFC_cst=128)
     if args.impl == "reference":

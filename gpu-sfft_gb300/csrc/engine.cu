@@ -106,7 +106,9 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   A(topk_idx, sizeof(int) * (size_t)p.k + 16);
   A(topk, sizeof(DevNode) * (size_t)p.k + 16);
   A(ctl, sizeof(RunCtl));
+  A(rmax, sizeof(unsigned long long) * (size_t)(p.RLFC_loops + p.loops));
 #undef A
+  P->floor_rel = (flags & GSFFT_FLAG_RAW_SELECTION) ? 0.0 : 1e-10;
   if (s == GSFFT_OK) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
   if (s == GSFFT_OK) s = fft_plan_init(P->fftW, p.W_RLFC, precision, p.RLFC_loops);
   if (s == GSFFT_OK) s = select_scratch_init(P->selB, p.loops_loc, p.B);
@@ -134,7 +136,7 @@ void plan_destroy(Plan *P) {
   if (!P) return;
   void *ptrs[] = {P->filt, P->hinv, P->rsamp, P->J2b, P->J2, P->bins, P->bsamp, P->J,
                   P->bm_j2, P->bm_sig, P->tile_tmp, P->vote, P->cand, P->cnt, P->blk,
-                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl};
+                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
@@ -193,6 +195,10 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   }
   GS_CUDA(cudaMemsetAsync(P->ctl, 0, sizeof(RunCtl), st));
   const int kb = P->precision == GSFFT_FP64 ? 8 : 4;
+  GS_CUDA(cudaMemsetAsync(P->rmax, 0, sizeof(unsigned long long) * (p.RLFC_loops + p.loops), st));
+  // row maxima as u64 (FP64) or u32 (FP32) arrays
+  void *rmax_w = P->rmax;
+  void *rmax_b = (char *)P->rmax + (size_t)kb * p.RLFC_loops;
   cudaEvent_t *ev = nullptr;
   if (P->timing && P->timed_runs < 512) {
     const size_t need = (size_t)(P->timed_runs + 1) * (ST_COUNT + 1);
@@ -215,11 +221,12 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
     for (int r = 0; r < p.RLFC_loops; r++) io.gather_offsets[r] = d.offs[r];
     io.gather_stride = p.n / p.W_RLFC;
     io.samples = P->rsamp;
+    io.row_max = rmax_w;
     io.write_complex = false;
     GS_CHECK(fft_exec(P->fftW, nullptr, P->rsamp, p.RLFC_loops, -1, io, st));
     MARK(1);
     GS_CHECK(select_top(P->rsamp, kb, p.W_RLFC, nullptr, p.B_thresh, p.RLFC_loops, p.W_RLFC,
-                        P->J2b, p.B_thresh, nullptr, P->selW, st));
+                        P->J2b, p.B_thresh, nullptr, P->selW, st, rmax_w, P->floor_rel));
     MARK(2);
     GS_CHECK(launch_j2_merge(P->J2b, p.RLFC_loops * p.B_thresh, p.W_RLFC, P->bm_j2, P->J2, P->ctl,
                              P->tile_tmp, st));
@@ -234,11 +241,12 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   {
     FftIo io;
     io.samples = P->bsamp;
+    io.row_max = rmax_b;
     GS_CHECK(fft_exec(P->fftB, P->bins, P->bins, p.loops, -1, io, st));
   }
   MARK(5);
   GS_CHECK(select_top(P->bsamp, kb, p.B, nullptr, p.B_thresh, p.loops_loc, p.B, P->J, p.B_thresh,
-                      nullptr, P->selB, st));
+                      nullptr, P->selB, st, rmax_b, P->floor_rel));
   MARK(6);
   // A7: voting, one location loop after the other
   const size_t wW = (size_t)p.W_RLFC / 32;

@@ -37,6 +37,8 @@ struct Plan {
   int *topk_idx = nullptr;
   DevNode *topk = nullptr;
   RunCtl *ctl = nullptr;
+  void *rmax = nullptr;  // per-row maxima: RLFC_loops rows then loops rows (u64 each)
+  double floor_rel = 1e-10;
   // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
   bool timing = false;
   std::vector<cudaEvent_t> events;  // (ST_COUNT + 1) per recorded run

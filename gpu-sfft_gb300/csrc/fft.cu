@@ -151,11 +151,37 @@ struct PassArgs {
   long long goffs[8];
   long long gstride;
   void *samples;      // last pass only, or null
+  void *row_max;      // per batch row, with samples
   int write_complex;
 };
 
 __device__ __forceinline__ double sq_sum(double2 v) { return __dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)); }
 __device__ __forceinline__ float sq_sum(float2 v) { return __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)); }
+
+__device__ __forceinline__ unsigned long long key_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+__device__ __forceinline__ unsigned key_bits(float v) { return __float_as_uint(v); }
+
+// atomic max of a non-negative sample over a warp segment of one batch row
+__device__ __forceinline__ void row_max_update(void *rm, long long b, double v) {
+  unsigned long long k = (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long y = __shfl_down_sync(0xffffffffu, k, o);
+    k = y > k ? y : k;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long *>(rm) + b, k);
+}
+__device__ __forceinline__ void row_max_update(void *rm, long long b, float v) {
+  unsigned k = __float_as_uint(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned y = __shfl_down_sync(0xffffffffu, k, o);
+    k = y > k ? y : k;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned *>(rm) + b, k);
+}
 
 template <typename T, int LOGR>
 __global__ void __launch_bounds__(nt_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
@@ -192,17 +218,31 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   cta_fft<V, LOGR, G>(sm, reinterpret_cast<const V *>(a.twR));
   V *__restrict__ out = reinterpret_cast<V *>(a.out);
   T *__restrict__ smp = reinterpret_cast<T *>(a.samples);
+  // R * G is a multiple of NT, so every warp runs the same trip count and
+  // its 32 lanes always hold elements of one batch row (R >= 128 > 32)
   for (int lt = threadIdx.x; lt < R * G; lt += NT) {
     int g, k;
     if (a.Ns >= G) { g = lt % G; k = lt / G; } else { k = lt % R; g = lt / R; }
     const long long u = u0 + g;
-    if (u >= a.total) continue;
+    const bool live = u < a.total;
     const long long b = u / S, j = u - b * S;
-    const long long dest = (j / a.Ns) * a.Ns * R + (j % a.Ns) + (long long)k * a.Ns;
-    V v = sm[g * RP + padded(k)];
-    if (a.inverse) v.y = -v.y;
-    if (a.write_complex) out[b * a.bstride + dest] = v;
-    if (smp) smp[b * a.bstride + dest] = sq_sum(v);
+    T sv = 0;
+    if (live) {
+      const long long dest = (j / a.Ns) * a.Ns * R + (j % a.Ns) + (long long)k * a.Ns;
+      V v = sm[g * RP + padded(k)];
+      if (a.inverse) v.y = -v.y;
+      if (a.write_complex) out[b * a.bstride + dest] = v;
+      if (smp) {
+        sv = sq_sum(v);
+        smp[b * a.bstride + dest] = sv;
+      }
+    }
+    if (smp && a.row_max) {
+      const long long bb = __shfl_sync(0xffffffffu, b, 0);
+      const bool uniform = __all_sync(0xffffffffu, b == bb && live);
+      if (uniform) row_max_update(a.row_max, bb, sv);
+      else if (live) atomicMax(reinterpret_cast<typename KeyOf<T>::K *>(a.row_max) + b, key_bits(sv));
+    }
   }
 }
 
@@ -365,6 +405,7 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
     for (int q = 0; q < 8; q++) a.goffs[q] = io.gather_offsets[q];
     a.gstride = io.gather_stride;
     a.samples = last ? io.samples : nullptr;
+    a.row_max = last ? io.row_max : nullptr;
     a.write_complex = last ? (io.write_complex ? 1 : 0) : 1;
     const long long total_sub = (p.n >> p.logR[i]) * batch;
     a.total = total_sub;

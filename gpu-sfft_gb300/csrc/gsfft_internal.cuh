@@ -90,6 +90,9 @@ struct FftIo {
   long long gather_stride = 0;
   // epilogue: |X|^2 (same precision) written to samples[b * n + k]
   void *samples = nullptr;
+  // optional: per-row maximum of the samples (bit pattern, u64 for double /
+  // u32 for float) accumulated with atomicMax; the caller zeroes it first
+  void *row_max = nullptr;
   bool write_complex = true;
 };
 
@@ -114,9 +117,13 @@ struct SelectScratch {
 };
 int select_scratch_init(SelectScratch &s, int max_batch, long long max_size);
 void select_scratch_free(SelectScratch &s);
+// row_max (optional, per row, bit pattern of the largest sample) with
+// floor_rel > 0: samples below floor_rel * max are taken as exact zeros, so
+// rounding-level samples tie and resolve by ascending index.
 int select_top(const void *keys, int key_bytes, long long size, const int *size_dev,
                int num, int batch, long long row_stride, int *out, long long out_stride,
-               int *count_out, SelectScratch &s, cudaStream_t st);
+               int *count_out, SelectScratch &s, cudaStream_t st,
+               const void *row_max = nullptr, double floor_rel = 0.0);
 int select_launches(int key_bytes);
 
 // ---------------------------------------------------------------- misc kernels

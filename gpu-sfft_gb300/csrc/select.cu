@@ -16,6 +16,12 @@
 //   3. One writing pass: sample i is taken iff key > thr, or key == thr and
 //      fewer than num - #greater equal keys precede it; its output slot is the
 //      number of taken samples before it, so ids come out ascending.
+// Optional rounding floor: with the row maximum known, samples below
+// floor_rel * max are read as exact zeros.  In a noiseless signal most RLFC
+// bins are zero in exact arithmetic and an FFT leaves them at rounding level;
+// the floor makes their ties resolve by index, the reference's own tie rule,
+// instead of by rounding noise, so FP64, FP32 and the CPU oracle pick the
+// same ids.
 #include "gsfft_internal.cuh"
 
 namespace gsfft {
@@ -28,6 +34,7 @@ constexpr int SEL_TILE = SEL_THREADS * SEL_ITEMS;
 constexpr int HIST_BINS = 2048;
 
 struct SelState {
+  unsigned long long floor;   // keys below this count as 0 (0 = no floor)
   unsigned long long prefix;  // key bits decided so far
   long long rank;             // ascending rank still to find inside the prefix
   int size;                   // live size of the row
@@ -38,16 +45,21 @@ struct SelState {
   int pad;
 };
 
-template <typename K> __device__ __forceinline__ K load_key(const void *p, long long i);
-template <> __device__ __forceinline__ unsigned long long load_key<unsigned long long>(const void *p, long long i) {
+template <typename K> __device__ __forceinline__ K raw_key(const void *p, long long i);
+template <> __device__ __forceinline__ unsigned long long raw_key<unsigned long long>(const void *p, long long i) {
   return (unsigned long long)__double_as_longlong(__ldg(reinterpret_cast<const double *>(p) + i));
 }
-template <> __device__ __forceinline__ unsigned int load_key<unsigned int>(const void *p, long long i) {
+template <> __device__ __forceinline__ unsigned int raw_key<unsigned int>(const void *p, long long i) {
   return __float_as_uint(__ldg(reinterpret_cast<const float *>(p) + i));
 }
+template <typename K> __device__ __forceinline__ K load_key(const void *p, long long i, K floor) {
+  const K k = raw_key<K>(p, i);
+  return k < floor ? (K)0 : k;
+}
 
+template <typename K>
 __global__ void sel_init_kernel(SelState *st, unsigned *hist, long long size, const int *size_dev,
-                                int num) {
+                                int num, const void *row_max, double floor_rel) {
   const int b = blockIdx.x;
   for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) hist[(long long)b * HIST_BINS + i] = 0;
   if (threadIdx.x == 0) {
@@ -58,6 +70,17 @@ __global__ void sel_init_kernel(SelState *st, unsigned *hist, long long size, co
       if (sz < 0) sz = 0;
     }
     SelState s;
+    s.floor = 0;
+    if (row_max && floor_rel > 0.0) {
+      // floor = (T)(max * floor_rel), the product rounded in double
+      if (sizeof(K) == 8) {
+        const double m = __longlong_as_double((long long)reinterpret_cast<const unsigned long long *>(row_max)[b]);
+        s.floor = (unsigned long long)__double_as_longlong(m * floor_rel);
+      } else {
+        const float m = __uint_as_float(reinterpret_cast<const unsigned *>(row_max)[b]);
+        s.floor = __float_as_uint((float)((double)m * floor_rel));
+      }
+    }
     s.prefix = 0;
     s.size = (int)sz;
     s.take_all = sz <= num ? 1 : 0;
@@ -110,6 +133,7 @@ sel_hist_kernel(const void *keys, long long row_stride, SelState *st, unsigned *
   if (s->take_all) return;
   const int size = s->size;
   const unsigned long long prefix = s->prefix;
+  const K floor = (K)s->floor;
   const int kb = (int)sizeof(K) * 8;
   const unsigned long long hi_mask =
       (shift + width >= kb) ? 0ull : (~0ull << (shift + width)) & (kb == 64 ? ~0ull : 0xffffffffull);
@@ -122,7 +146,7 @@ sel_hist_kernel(const void *keys, long long row_stride, SelState *st, unsigned *
   for (int it = 0; it < SEL_ITEMS; it++) {
     const long long i = base + it * SEL_THREADS + threadIdx.x;
     if (i < size) {
-      const unsigned long long k = (unsigned long long)load_key<K>(row, i);
+      const unsigned long long k = (unsigned long long)load_key<K>(row, i, floor);
       if ((k & hi_mask) == prefix) atomicAdd(&sh[(unsigned)(k >> shift) & dmask], 1u);
     }
   }
@@ -177,6 +201,7 @@ sel_count_kernel(const void *keys, long long row_stride, SelState *st, unsigned 
   if (s->take_all) return;
   const int size = s->size;
   const K thr = (K)s->prefix;
+  const K floor = (K)s->floor;
   const long long base = (long long)blockIdx.x * SEL_TILE;
   const void *row = reinterpret_cast<const char *>(keys) + (size_t)b * row_stride * sizeof(K);
   unsigned gt = 0, eq = 0;
@@ -184,7 +209,7 @@ sel_count_kernel(const void *keys, long long row_stride, SelState *st, unsigned 
   for (int it = 0; it < SEL_ITEMS; it++) {
     const long long i = base + it * SEL_THREADS + threadIdx.x;
     if (i < size) {
-      const K k = load_key<K>(row, i);
+      const K k = load_key<K>(row, i, floor);
       gt += k > thr;
       eq += k == thr;
     }
@@ -249,6 +274,7 @@ sel_write_kernel(const void *keys, long long row_stride, const SelState *st, con
     return;
   }
   const K thr = (K)s->prefix;
+  const K floor = (K)s->floor;
   const unsigned *tb = tiles + (size_t)b * max_tiles * 4;
   unsigned gt_run = tb[blockIdx.x * 4 + 2];
   unsigned eq_run = tb[blockIdx.x * 4 + 3];
@@ -258,7 +284,7 @@ sel_write_kernel(const void *keys, long long row_stride, const SelState *st, con
     const long long i = base + it * SEL_THREADS + threadIdx.x;
     unsigned g = 0, e = 0;
     if (i < size) {
-      const K k = load_key<K>(row, i);
+      const K k = load_key<K>(row, i, floor);
       g = k > thr;
       e = k == thr;
     }
@@ -279,14 +305,14 @@ sel_write_kernel(const void *keys, long long row_stride, const SelState *st, con
 template <typename K>
 int select_impl(const void *keys, long long size, const int *size_dev, int num, int batch,
                 long long row_stride, int *out, long long out_stride, int *count_out,
-                SelectScratch &s, cudaStream_t st) {
+                SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
   if (batch > s.max_batch || size <= 0) return GSFFT_ERR_PARAM;
   const long long tiles = (size + SEL_TILE - 1) / SEL_TILE;
   if (tiles > s.max_tiles) return GSFFT_ERR_PARAM;
   SelState *state = reinterpret_cast<SelState *>(s.state);
   unsigned *hist = reinterpret_cast<unsigned *>(s.hist);
   unsigned *tl = reinterpret_cast<unsigned *>(s.tiles);
-  sel_init_kernel<<<batch, 256, 0, st>>>(state, hist, size, size_dev, num);
+  sel_init_kernel<K><<<batch, 256, 0, st>>>(state, hist, size, size_dev, num, row_max, floor_rel);
   GS_LAUNCHED();
   dim3 grid((unsigned)tiles, (unsigned)batch);
   const int kb = (int)sizeof(K) * 8;
@@ -332,14 +358,14 @@ int select_launches(int key_bytes) { return key_bytes == 8 ? 9 : 6; }
 
 int select_top(const void *keys, int key_bytes, long long size, const int *size_dev, int num,
                int batch, long long row_stride, int *out, long long out_stride, int *count_out,
-               SelectScratch &s, cudaStream_t st) {
+               SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
   if (size_dev && batch != 1) return GSFFT_ERR_PARAM;
   if (key_bytes == 8)
     return select_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride, out,
-                                           out_stride, count_out, s, st);
+                                           out_stride, count_out, s, st, row_max, floor_rel);
   if (key_bytes == 4)
     return select_impl<unsigned int>(keys, size, size_dev, num, batch, row_stride, out,
-                                     out_stride, count_out, s, st);
+                                     out_stride, count_out, s, st, row_max, floor_rel);
   return GSFFT_ERR_PARAM;
 }
 

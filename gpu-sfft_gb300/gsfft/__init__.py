@@ -21,6 +21,8 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "gsfft.h")
 
 FP64, MIXED = 0, 1
 FLAG_QUIRK_RESIDUE = 1
+FLAG_RAW_SELECTION = 2
+SELECTION_FLOOR = 1e-10
 OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE = range(7)
 
 NODE = np.dtype({"names": ["key", "x", "y"], "formats": ["<u4", "<f8", "<f8"],

@@ -50,6 +50,11 @@ typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
 /* Plan flags. */
 #define GSFFT_FLAG_QUIRK_RESIDUE 1u  /* reproduce permFilterTillKernel's residue
                                         tap index (innerLoop.cu:745-754) */
+#define GSFFT_FLAG_RAW_SELECTION 2u  /* cutoffs on the raw |X|^2 values.  By
+   default samples below 1e-10 x the row maximum count as exact zeros in the
+   RLFC and bucket cutoffs, so that bins which are zero in exact arithmetic
+   (half the RLFC picks of a noiseless signal) tie and resolve by ascending
+   index, the reference's tie rule, instead of by FFT rounding noise. */
 
 /* Run parameters derived exactly as experiment.c:71-84 and
  * cuExperiment.cu:279-284 derive them. */

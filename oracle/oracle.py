@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
 
 QUIRK_RESIDUE = 1
 QUIRK_FILTER_RECURRENCE = 2
+# the engine's default selection floor (samples below 1e-10 x max count as 0)
+SELECTION_FLOOR = 1e-10
 
 COMPLEX = np.dtype([("x", "<f8"), ("y", "<f8")])
 NODE = np.dtype({"names": ["key", "x", "y"], "formats": ["<u4", "<f8", "<f8"],
@@ -57,9 +59,13 @@ def lib():
         L.oc_cutoff_f64.restype = None
         L.oc_cutoff_f32.argtypes = [P, i, i, P]
         L.oc_cutoff_f32.restype = None
+        L.oc_cutoff_floor_f64.argtypes = [P, i, i, d, P]
+        L.oc_cutoff_floor_f64.restype = None
+        L.oc_cutoff_floor_f32.argtypes = [P, i, i, d, P]
+        L.oc_cutoff_floor_f32.restype = None
         L.oc_samples.argtypes = [P, i, P]
         L.oc_samples.restype = None
-        L.oc_rlfc.argtypes = [P, i, i, i, i, P, P]
+        L.oc_rlfc.argtypes = [P, i, i, i, i, d, P, P]
         L.oc_merge_j2.argtypes = [P, i]
         L.oc_perm_filter.argtypes = [P, i, P, i, i, i, C.c_uint, P]
         L.oc_perm_filter.restype = None
@@ -67,7 +73,7 @@ def lib():
         L.oc_estimate.argtypes = [P, i, P, i, i, P, i, P, P]
         L.oc_estimate.restype = None
         L.oc_topk.argtypes = [P, i, i, P]
-        L.oc_outer_loop.argtypes = [P, C.POINTER(Params), P, P, P, P, P, C.c_uint,
+        L.oc_outer_loop.argtypes = [P, C.POINTER(Params), P, P, P, P, P, C.c_uint, d,
                                     P, i, P, P, P, P, P]
         L.oc_mod_inverse.argtypes = [i, i]
         L.oc_gcd.argtypes = [i, i]
@@ -122,22 +128,22 @@ def samples(v):
     return s
 
 
-def cutoff(s, num):
+def cutoff(s, num, floor_rel=0.0):
     out = np.zeros(num, np.int32)
     if s.dtype == np.float32:
         s = np.ascontiguousarray(s)
-        lib().oc_cutoff_f32(_p(s), s.size, num, _p(out))
+        lib().oc_cutoff_floor_f32(_p(s), s.size, num, floor_rel, _p(out))
     else:
         s = np.ascontiguousarray(s, dtype=np.float64)
-        lib().oc_cutoff_f64(_p(s), s.size, num, _p(out))
+        lib().oc_cutoff_floor_f64(_p(s), s.size, num, floor_rel, _p(out))
     return out
 
 
-def rlfc(x, n, W, B_thresh, offset, want_spectrum=False):
+def rlfc(x, n, W, B_thresh, offset, want_spectrum=False, floor_rel=SELECTION_FLOOR):
     x = as_c128(x)
     J2 = np.zeros(B_thresh, np.int32)
     yf = np.zeros(W, np.complex128) if want_spectrum else None
-    st = lib().oc_rlfc(_p(x), n, W, B_thresh, offset, _p(J2), _p(yf))
+    st = lib().oc_rlfc(_p(x), n, W, B_thresh, offset, floor_rel, _p(J2), _p(yf))
     assert st == 0
     return (J2, yf) if want_spectrum else J2
 
@@ -191,7 +197,9 @@ def topk(nodes, k):
 
 
 def outer_loop(x, p, filter_time, filter_freq, offsets, a, ai, quirks=0, cap=1 << 22,
-               want_stages=False):
+               want_stages=False, floor_rel=SELECTION_FLOOR):
+    """The whole pipeline.  floor_rel: the engine's selection floor (default);
+    0 gives the reference's raw cutoffs."""
     x = as_c128(x)
     ft, ff = as_c128(filter_time), as_c128(filter_freq)
     offsets = np.ascontiguousarray(offsets, np.int32)
@@ -204,7 +212,7 @@ def outer_loop(x, p, filter_time, filter_freq, offsets, a, ai, quirks=0, cap=1 <
     bins = np.zeros(p.loops * p.B, np.complex128) if want_stages else None
     J = np.zeros(p.loops_loc * p.B_thresh, np.int32) if want_stages else None
     st = lib().oc_outer_loop(_p(x), C.byref(p), _p(ft), _p(ff), _p(offsets), _p(a), _p(ai),
-                             quirks, _p(out), cap, C.byref(I_F), _p(J2), C.byref(nrl),
+                             quirks, floor_rel, _p(out), cap, C.byref(I_F), _p(J2), C.byref(nrl),
                              _p(bins), _p(J))
     res = {"status": st, "nodes": out[:min(I_F.value, cap)].copy(), "I_F": I_F.value,
            "num_RLFC": nrl.value}

@@ -412,6 +412,30 @@ void oc_cutoff_f32(const float *samples, int size, int num, int *out) {
   free(d);
 }
 
+/* The engine's rounding floor (not in the reference): a noiseless signal
+ * leaves most RLFC bins at FFT rounding level; reading everything below
+ * floor_rel * max as 0 lets those ties resolve by index (the rule above). */
+void oc_cutoff_floor_f64(const double *samples, int size, int num, double floor_rel, int *out) {
+  if (floor_rel <= 0.0) { oc_cutoff_f64(samples, size, num, out); return; }
+  double mx = 0.0;
+  for (int i = 0; i < size; i++) mx = samples[i] > mx ? samples[i] : mx;
+  const double fl = mx * floor_rel;
+  double *d = (double *)malloc(sizeof(double) * (size_t)size);
+  for (int i = 0; i < size; i++) d[i] = samples[i] < fl ? 0.0 : samples[i];
+  oc_cutoff_f64(d, size, num, out);
+  free(d);
+}
+
+void oc_cutoff_floor_f32(const float *samples, int size, int num, double floor_rel, int *out) {
+  float mx = 0.0f;
+  for (int i = 0; i < size; i++) mx = samples[i] > mx ? samples[i] : mx;
+  const float fl = floor_rel > 0.0 ? (float)((double)mx * floor_rel) : 0.0f;
+  double *d = (double *)malloc(sizeof(double) * (size_t)size);
+  for (int i = 0; i < size; i++) d[i] = samples[i] < fl ? 0.0 : (double)samples[i];
+  oc_cutoff_f64(d, size, num, out);
+  free(d);
+}
+
 /* samplesKernel (innerLoop.cu:708-718): re^2 + im^2, each product rounded. */
 void oc_samples(const oc_complex *v, int size, double *s) {
 #pragma omp parallel for schedule(static) if (size >= 65536)
@@ -424,7 +448,7 @@ void oc_samples(const oc_complex *v, int size, double *s) {
 
 /* innerLoop.cu:112-161 and restLocFreqCoeffKernel :693-703. */
 int oc_rlfc(const oc_complex *x, int n, int W_RLFC, int B_thresh, int offset,
-            int *J2_block, oc_complex *y_f) {
+            double floor_rel, int *J2_block, oc_complex *y_f) {
   const int sigma = n / W_RLFC;
   oc_complex *y = (oc_complex *)malloc(sizeof(oc_complex) * (size_t)W_RLFC);
   double *s = (double *)malloc(sizeof(double) * (size_t)W_RLFC);
@@ -433,7 +457,7 @@ int oc_rlfc(const oc_complex *x, int n, int W_RLFC, int B_thresh, int offset,
   int st = oc_fft(y, W_RLFC, -1);
   if (st == OC_OK) {
     oc_samples(y, W_RLFC, s);
-    oc_cutoff_f64(s, W_RLFC, B_thresh, J2_block);
+    oc_cutoff_floor_f64(s, W_RLFC, B_thresh, floor_rel, J2_block);
     if (y_f) memcpy(y_f, y, sizeof(oc_complex) * (size_t)W_RLFC);
   }
   free(y); free(s);
@@ -645,7 +669,7 @@ int oc_topk(const oc_node *nodes, int num, int k, oc_node *out) {
 int oc_outer_loop(const oc_complex *x, const oc_params *p,
                   const oc_complex *filter_time, const oc_complex *filter_freq,
                   const int *rlfc_offsets, const int *a, const int *ai,
-                  unsigned quirks, oc_node *out, int cap, int *I_F,
+                  unsigned quirks, double floor_rel, oc_node *out, int cap, int *I_F,
                   int *J2_out, int *num_RLFC_out, oc_complex *bins_f_out,
                   int *J_out) {
   const int n = p->n, B = p->B, Bt = p->B_thresh, W = p->W_RLFC;
@@ -659,7 +683,7 @@ int oc_outer_loop(const oc_complex *x, const oc_params *p,
   int *cand = (int *)malloc(sizeof(int) * (size_t)(cap > 0 ? cap : 1));
   if (!J2 || !bins_f || !s || !J || !vote || !cand) { st = OC_ERR_ALLOC; goto done; }
   for (int r = 0; r < p->RLFC_loops && st == OC_OK; r++)
-    st = oc_rlfc(x, n, W, Bt, rlfc_offsets[r], J2 + (size_t)r * Bt, NULL);
+    st = oc_rlfc(x, n, W, Bt, rlfc_offsets[r], floor_rel, J2 + (size_t)r * Bt, NULL);
   if (st != OC_OK) goto done;
   if (J2_out) memcpy(J2_out, J2, sizeof(int) * (size_t)p->RLFC_loops * Bt);
   int num_RLFC = Bt;
@@ -673,7 +697,7 @@ int oc_outer_loop(const oc_complex *x, const oc_params *p,
     if (st != OC_OK) goto done;
     if (i < p->loops_loc) {
       oc_samples(bf, B, s);
-      oc_cutoff_f64(s, B, Bt, J);
+      oc_cutoff_floor_f64(s, B, Bt, floor_rel, J);
       if (J_out) memcpy(J_out + (size_t)i * Bt, J, sizeof(int) * (size_t)Bt);
       int rs = oc_reverse_hash(J, Bt, J2, num_RLFC, n, B, W, a[i], ai[i],
                                p->loops_thresh, vote, cand, &num_cand, cap);

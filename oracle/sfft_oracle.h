@@ -75,13 +75,18 @@ int  oc_design_filter(const oc_params *p, unsigned quirks,
 /* A6 cutoff: indices of the num largest samples, ascending (innerLoop.cu:551-616). */
 void oc_cutoff_f64(const double *samples, int size, int num, int *out);
 void oc_cutoff_f32(const float *samples, int size, int num, int *out);
+/* Same with the engine's rounding floor: samples below floor_rel * max are
+ * taken as exact zeros (floor = max * floor_rel rounded in double, then to the
+ * sample type). floor_rel = 0 is the plain cutoff. */
+void oc_cutoff_floor_f64(const double *samples, int size, int num, double floor_rel, int *out);
+void oc_cutoff_floor_f32(const float *samples, int size, int num, double floor_rel, int *out);
 
 /* |v|^2 without contraction (innerLoop.cu:715). */
 void oc_samples(const oc_complex *v, int size, double *samples);
 
 /* A4 one RLFC loop (innerLoop.cu:112-161 + :693-703): J2 block of B_thresh ids. */
 int  oc_rlfc(const oc_complex *x, int n, int W_RLFC, int B_thresh, int offset,
-             int *J2_block, oc_complex *y_f /* W_RLFC or NULL */);
+             double floor_rel, int *J2_block, oc_complex *y_f /* W_RLFC or NULL */);
 
 /* Sorted, de-duplicated union of RLFC_loops blocks (outerLoop.cu:111-121). */
 int  oc_merge_j2(int *J2, int total);
@@ -111,7 +116,7 @@ int  oc_topk(const oc_node *nodes, int num, int k, oc_node *out);
 int  oc_outer_loop(const oc_complex *x, const oc_params *p,
                    const oc_complex *filter_time, const oc_complex *filter_freq,
                    const int *rlfc_offsets, const int *a, const int *ai,
-                   unsigned quirks, oc_node *out, int cap, int *I_F,
+                   unsigned quirks, double floor_rel, oc_node *out, int cap, int *I_F,
                    int *J2_out, int *num_RLFC_out, oc_complex *bins_f_out,
                    int *J_out);
 

@@ -20,6 +20,18 @@ def dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
+def recovered(top, loc):
+    """True locations present in a top-k list.
+
+    With a noiseless signal about half of the RLFC picks are bins that are
+    exactly zero in exact arithmetic; which of them an FFT selects depends on
+    its rounding, so two correct FFTs yield different false candidates (and,
+    when the randomised method loses a true location, different top-k
+    fillers).  End to end, the recovered true locations are compared; with
+    inputs fed stage by stage, the index outputs are compared bit for bit."""
+    return set(top["key"].tolist()) & set(int(v) for v in loc)
+
+
 def setup(G, O, torch, cfg, seed=0, snr_db=None):
     p_o, st = O.derive_params(*cfg)
     assert st == 0
@@ -69,7 +81,8 @@ def test_fp64_pipeline_vs_oracle(G, O, torch_cuda, name):
     assert np.abs(st["bins"] - bins_o).max() <= 1e-11 * np.abs(bins_o).max()
     # stage injection: the oracle's cutoff on the GPU's bins gives the GPU's J
     for l in range(p.loops_loc):
-        np.testing.assert_array_equal(st["J"][l], O.cutoff(O.samples(st["bins"][l]), p.B_thresh))
+        np.testing.assert_array_equal(
+            st["J"][l], O.cutoff(O.samples(st["bins"][l]), p.B_thresh, floor_rel=G.SELECTION_FLOOR))
     # stage injection: the oracle's vote on the GPU's J and J2 gives the GPU's
     # candidates in the same (canonical) order
     vote = np.zeros(p.n, np.int32)
@@ -86,11 +99,30 @@ def test_fp64_pipeline_vs_oracle(G, O, torch_cuda, name):
     # end to end: the recovered (top-k) location set is identical, values 1e-9
     top_o = O.topk(o["nodes"], p.k)
     top_g = g["topk"]
-    assert set(top_g["key"].tolist()) == set(top_o["key"].tolist())
+    rec = recovered(top_g, loc)
+    assert rec == recovered(top_o, loc)
+    assert len(rec) >= p.k - 3
     vo = dict(zip(top_o["key"].tolist(), top_o["x"] + 1j * top_o["y"]))
-    vg = np.array([vo[k] for k in top_g["key"].tolist()])
-    got = top_g["x"] + 1j * top_g["y"]
+    common = [r for r in top_g if int(r["key"]) in vo]
+    vg = np.array([vo[int(r["key"])] for r in common])
+    got = np.array([complex(r["x"], r["y"]) for r in common])
     assert np.abs(got - vg).max() <= 1e-9 * np.abs(vg).max()
+
+
+def test_fp64_pipeline_noisy_exact(G, O, torch_cuda):
+    """With 40 dB noise no RLFC pick sits at rounding level: the whole top-k
+    list (keys and order) matches the oracle, values within 1e-9."""
+    torch = torch_cuda
+    p, p_g, x, loc, X, ft, ff, (offs, a, ai) = setup(G, O, torch, CFGS["config1"], seed=2,
+                                                     snr_db=40.0)
+    g = run_gpu(G, torch, p_g, x, ft, ff, (offs, a, ai))
+    o = O.outer_loop(x, p, ft, ff, offs, a, ai)
+    np.testing.assert_array_equal(g["nodes"]["key"], o["nodes"]["key"])
+    top_o = O.topk(o["nodes"], p.k)
+    np.testing.assert_array_equal(g["topk"]["key"], top_o["key"])
+    vo = top_o["x"] + 1j * top_o["y"]
+    vg = g["topk"]["x"] + 1j * g["topk"]["y"]
+    assert np.abs(vg - vo).max() <= 1e-9 * np.abs(vo).max()
 
 
 @pytest.mark.parametrize("name", ["n16", "config1"])
@@ -101,7 +133,7 @@ def test_fp64_residue_quirk(G, O, torch_cuda, name):
     g = run_gpu(G, torch, p_g, x, ft, ff, (offs, a, ai), flags=G.FLAG_QUIRK_RESIDUE)
     o = O.outer_loop(x, p, ft, ff, offs, a, ai, quirks=O.QUIRK_RESIDUE, want_stages=True)
     assert np.abs(g["stages"]["bins"] - o["bins_f"]).max() <= 1e-11 * np.abs(o["bins_f"]).max()
-    assert set(g["topk"]["key"].tolist()) == set(O.topk(o["nodes"], p.k)["key"].tolist())
+    assert recovered(g["topk"], loc) == recovered(O.topk(o["nodes"], p.k), loc)
 
 
 def test_deterministic_repeat(G, O, torch_cuda):
@@ -128,10 +160,15 @@ def test_mixed_vs_fp64(G, O, torch_cuda, name, snr):
     g64 = run_gpu(G, torch, p_g, x, ft, ff, draws, prec=0)
     g32 = run_gpu(G, torch, p_g, x, ft, ff, draws, prec=1)
     k64 = g64["topk"]["key"].tolist()
+    # the selection floor makes rounding-level picks identical across precisions
+    np.testing.assert_array_equal(g32["stages"]["J2"], g64["stages"]["J2"])
+    np.testing.assert_array_equal(g32["nodes"]["key"], g64["nodes"]["key"])
     assert set(g32["topk"]["key"].tolist()) == set(k64)
+    assert recovered(g32["topk"], loc) == recovered(g64["topk"], loc)
     v64 = dict(zip(k64, g64["topk"]["x"] + 1j * g64["topk"]["y"]))
-    v32 = np.array([complex(r["x"], r["y"]) for r in g32["topk"]])
-    ref = np.array([v64[k] for k in g32["topk"]["key"].tolist()])
+    common = [r for r in g32["topk"] if int(r["key"]) in v64]
+    v32 = np.array([complex(r["x"], r["y"]) for r in common])
+    ref = np.array([v64[int(r["key"])] for r in common])
     rel = np.linalg.norm(v32 - ref) / np.linalg.norm(ref)
     assert rel <= 1e-5, rel
 
@@ -155,7 +192,7 @@ def test_outer_loop_dropin(G, O, torch_cuda):
     o = O.outer_loop(x, p, ft, ff, offs, a, ai, quirks=O.QUIRK_RESIDUE)
     top_o = O.topk(o["nodes"], p.k)
     top_g = O.topk(nodes, p.k)
-    assert set(top_g["key"].tolist()) == set(top_o["key"].tolist())
+    assert recovered(top_g, loc) == recovered(top_o, loc)
 
 
 def test_filter_design_gpu(G, O, torch_cuda):
@@ -176,11 +213,12 @@ def test_plan_rejects_bad_draws(G, O, torch_cuda):
     torch = torch_cuda
     p, p_g, x, loc, X, ft, ff, (offs, a, ai) = setup(G, O, torch, CFGS["n16"])
     plan = G.Plan(p_g, 0)
+    d_x, d_ft, d_ff = dev(torch, x), dev(torch, ft), dev(torch, ff)
     with pytest.raises(G.GsfftError):  # run before the filter is installed
-        plan.run(dev(torch, x).data_ptr(), offs, a, ai)
-    plan.set_filter(dev(torch, ft).data_ptr(), dev(torch, ff).data_ptr())
+        plan.run(d_x.data_ptr(), offs, a, ai)
+    plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
     bad = a.copy()
     bad[0] = 2  # even: not invertible mod 2^q
     with pytest.raises(G.GsfftError):
-        plan.run(dev(torch, x).data_ptr(), offs, bad, ai)
+        plan.run(d_x.data_ptr(), offs, bad, ai)
     plan.close()

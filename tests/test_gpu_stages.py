@@ -66,8 +66,9 @@ def test_perm_filter_bitexact_fp64(G, O, torch_cuda, quirk):
     f = rng.normal(size=w) + 1j * rng.normal(size=w)
     ai = (rng.integers(0, n // 2, size=9) * 2 + 1).astype(np.int32)
     d_bins = torch.zeros((9, B), dtype=torch.complex128, device="cuda")
-    G.stage_perm_filter(0, dev(torch, x).data_ptr(), n, dev(torch, f).data_ptr(), w, B, ai,
-                        d_bins.data_ptr(), quirk_residue=quirk)
+    d_x, d_f = dev(torch, x), dev(torch, f)  # keep the buffers alive across the call
+    G.stage_perm_filter(0, d_x.data_ptr(), n, d_f.data_ptr(), w, B, ai, d_bins.data_ptr(),
+                        quirk_residue=quirk)
     got = d_bins.cpu().numpy()
     for l in range(9):
         ref = O.perm_filter(x, n, f, B, int(ai[l]), quirks=1 if quirk else 0)
@@ -82,8 +83,8 @@ def test_perm_filter_fp32(G, O, torch_cuda):
     f = rng.normal(size=w) + 1j * rng.normal(size=w)
     ai = (rng.integers(0, n // 2, size=3) * 2 + 1).astype(np.int32)
     d_bins = torch.zeros((3, B), dtype=torch.complex64, device="cuda")
-    G.stage_perm_filter(1, dev(torch, x.astype(np.complex64)).data_ptr(), n,
-                        dev(torch, f).data_ptr(), w, B, ai, d_bins.data_ptr())
+    d_x, d_f = dev(torch, x.astype(np.complex64)), dev(torch, f)
+    G.stage_perm_filter(1, d_x.data_ptr(), n, d_f.data_ptr(), w, B, ai, d_bins.data_ptr())
     got = d_bins.cpu().numpy()
     for l in range(3):
         ref = O.perm_filter(x, n, f, B, int(ai[l]))
@@ -112,7 +113,8 @@ def test_reverse_hash_exact(G, O, torch_cuda, seed):
         c, vote_o, st = O.reverse_hash(J, J2, n, B, W, int(a[l]), int(ai[l]), 2, vote=vote_o,
                                        cand=cand_o)
         cand_o = list(c)
-        s, count = G.stage_reverse_hash(dev(torch, J).data_ptr(), J.size, d_J2.data_ptr(), J2.size,
+        d_J = dev(torch, J)
+        s, count = G.stage_reverse_hash(d_J.data_ptr(), J.size, d_J2.data_ptr(), J2.size,
                                         n, B, W, int(a[l]), int(ai[l]), 2, 0, d_vote.data_ptr(),
                                         d_cand.data_ptr(), 1 << 16, count)
         assert s == 0
@@ -127,7 +129,8 @@ def test_reverse_hash_capacity(G, torch_cuda):
     J = np.arange(0, B, 1, dtype=np.int32)[:200]
     d_vote = torch.zeros(n, dtype=torch.int32, device="cuda")
     d_cand = torch.full((64,), -7, dtype=torch.int32, device="cuda")
-    s, count = G.stage_reverse_hash(dev(torch, J).data_ptr(), J.size, dev(torch, J2).data_ptr(),
+    d_J, d_J2 = dev(torch, J), dev(torch, J2)
+    s, count = G.stage_reverse_hash(d_J.data_ptr(), J.size, d_J2.data_ptr(),
                                     J2.size, n, B, W, 3, pow(3, -1, n), 1, 0, d_vote.data_ptr(),
                                     d_cand.data_ptr(), 32, 0)
     assert s == G.ERR_CAPACITY and count > 32
@@ -147,9 +150,11 @@ def test_estimate(G, O, torch_cuda, prec):
         bins = bins.astype(np.complex64).astype(np.complex128)
     ref = O.estimate(cand, bins, loops, n, ai, B, ff)
     d_out = torch.zeros(cand.size * 3, dtype=torch.float64, device="cuda")
-    G.stage_estimate(prec, dev(torch, cand).data_ptr(), cand.size,
-                     dev(torch, bins.astype(np.complex128 if prec == 0 else np.complex64)).data_ptr(),
-                     loops, n, B, ai, dev(torch, ff).data_ptr(), d_out.data_ptr())
+    d_cand = dev(torch, cand)
+    d_bins = dev(torch, bins.astype(np.complex128 if prec == 0 else np.complex64))
+    d_ff = dev(torch, ff)
+    G.stage_estimate(prec, d_cand.data_ptr(), cand.size, d_bins.data_ptr(), loops, n, B, ai,
+                     d_ff.data_ptr(), d_out.data_ptr())
     got = d_out.cpu().numpy().view(G.NODE)
     np.testing.assert_array_equal(got["key"], ref["key"])
     scale = np.abs(ref["x"] + 1j * ref["y"]).max()
