@@ -257,7 +257,7 @@ int gsfft_stage_reverse_hash(const int *d_J, int B_thresh, const int *d_J2, int 
   int s = GSFFT_OK;
   if (cudaMalloc(&bm, sizeof(unsigned) * words) != cudaSuccess ||
       cudaMalloc(&cnt, sizeof(int) * B_thresh) != cudaSuccess ||
-      cudaMalloc(&blk, sizeof(int) * (B_thresh / 256 + 2)) != cudaSuccess ||
+      cudaMalloc(&blk, sizeof(int) * vote_block_ints(B_thresh)) != cudaSuccess ||
       cudaMalloc(&ctl, sizeof(RunCtl)) != cudaSuccess)
     s = GSFFT_ERR_ALLOC;
   Draws d;

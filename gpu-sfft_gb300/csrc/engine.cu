@@ -100,7 +100,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   A(vote, sizeof(unsigned) * (size_t)p.n);
   A(cand, sizeof(int) * (size_t)P->cap);
   A(cnt, sizeof(int) * (size_t)p.B_thresh);
-  A(blk, sizeof(int) * (size_t)(p.B_thresh / 256 + 2));
+  A(blk, sizeof(int) * (size_t)vote_block_ints(p.B_thresh));
   A(nodes, sizeof(DevNode) * (size_t)P->cap);
   A(mag2, sizeof(double) * (size_t)P->cap);
   A(topk_idx, sizeof(int) * (size_t)p.k + 16);

@@ -31,6 +31,57 @@ __device__ __forceinline__ double median_of(const double *v, int L) {
   return res;
 }
 
+// Compile-time loop count: the per-loop values live in registers.
+template <int L>
+__device__ __forceinline__ double median_reg(const double (&v)[L]) {
+  constexpr int want = (L - 1) / 2;
+  double res = v[0];
+#pragma unroll
+  for (int i = 0; i < L; i++) {
+    int rank = 0;
+#pragma unroll
+    for (int j = 0; j < L; j++) rank += (v[j] < v[i]) || (v[j] == v[i] && j < i);
+    if (rank == want) res = v[i];
+  }
+  return res;
+}
+
+template <typename T, int L>
+__global__ void __launch_bounds__(ET)
+estimate_kernel_fixed(const int *__restrict__ cand, const RunCtl *ctl, int cap,
+                      const typename Cx<T>::V *__restrict__ bins, unsigned nmask, int lognb, int B,
+                      Draws d, const double2 *__restrict__ hinv, DevNode *nodes, double *mag2) {
+  const int count = min(ctl->cand_count, cap);
+  const int nb = 1 << lognb;
+  for (int i = blockIdx.x * ET + threadIdx.x; i < count; i += gridDim.x * ET) {
+    const unsigned loc = (unsigned)cand[i];
+    double vr[L], vi[L];
+#pragma unroll
+    for (int j = 0; j < L; j++) {
+      const unsigned p = ((unsigned)d.ai[j] * loc) & nmask;
+      int h = (int)(p >> lognb);
+      int dd = (int)(p & (unsigned)(nb - 1));
+      if (dd > nb / 2) {
+        h = (h + 1) & (B - 1);
+        dd -= nb;
+      }
+      const double2 H = __ldg(&hinv[dd + nb / 2]);
+      const typename Cx<T>::V bv = bins[(size_t)j * B + h];
+      const double bx = (double)bv.x, by = (double)bv.y;
+      vr[j] = fma(bx, H.x, -(by * H.y));
+      vi[j] = fma(bx, H.y, by * H.x);
+    }
+    const double re = median_reg<L>(vr), im = median_reg<L>(vi);
+    DevNode nd;
+    nd.key = loc;
+    nd.pad = 0;
+    nd.x = re;
+    nd.y = im;
+    nodes[i] = nd;
+    mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(ET)
 estimate_kernel(const int *__restrict__ cand, const RunCtl *ctl, int cap,
@@ -80,6 +131,27 @@ int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, 
   int lognb = 0;
   while ((1 << lognb) < n / B) lognb++;
   const unsigned nmask = (unsigned)n - 1u;
+  if (loops >= 2 && loops <= 16) {
+    const int grid = min((cap + ET - 1) / ET, 152 * 8);
+#define EST_CASE(LL)                                                                            \
+  case LL:                                                                                      \
+    if (precision == GSFFT_FP64)                                                                \
+      estimate_kernel_fixed<double, LL><<<grid, ET, 0, st>>>(cand, ctl, cap, (const double2 *)bins, \
+                                                             nmask, lognb, B, d, hinv, nodes, mag2); \
+    else                                                                                        \
+      estimate_kernel_fixed<float, LL><<<grid, ET, 0, st>>>(cand, ctl, cap, (const float2 *)bins,   \
+                                                            nmask, lognb, B, d, hinv, nodes, mag2);  \
+    break;
+    switch (loops) {
+      EST_CASE(2) EST_CASE(3) EST_CASE(4) EST_CASE(5) EST_CASE(6) EST_CASE(7) EST_CASE(8)
+      EST_CASE(9) EST_CASE(10) EST_CASE(11) EST_CASE(12) EST_CASE(13) EST_CASE(14) EST_CASE(15)
+      EST_CASE(16)
+      default: break;
+    }
+#undef EST_CASE
+    GS_LAUNCHED();
+    return GSFFT_OK;
+  }
   const int grid = (cap + ET - 1) / ET;
   if (precision == GSFFT_FP64)
     estimate_kernel<double><<<grid, ET, 0, st>>>(cand, ctl, cap, (const double2 *)bins, loops,

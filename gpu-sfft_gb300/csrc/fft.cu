@@ -139,6 +139,8 @@ struct PassArgs {
   const void *in;
   void *out;
   long long N;        // transform size
+  int logN;           // log2 N
+  int logNs;          // log2 of the product of the earlier radices
   long long bstride;  // batch stride of in/out/samples (elements)
   int batch;
   long long total;    // sub-transforms over the whole batch
@@ -187,28 +189,46 @@ template <typename T, int LOGR>
 __global__ void __launch_bounds__(nt_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   typedef typename Cx<T>::V V;
   constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = padded(R);
+  constexpr int ITER = R * G / NT;  // elements per thread in the load / store phases
   extern __shared__ __align__(16) unsigned char smraw[];
   V *sm = reinterpret_cast<V *>(smraw);
   const V *__restrict__ in = reinterpret_cast<const V *>(a.in);
   const V *__restrict__ gx = reinterpret_cast<const V *>(a.gx);
   const V *__restrict__ thi = reinterpret_cast<const V *>(a.tw_hi);
   const V *__restrict__ tlo = reinterpret_cast<const V *>(a.tw_lo);
-  const long long S = a.N / R;
+  // all sizes are powers of two: S = N/R sub-transforms per batch entry
+  const int logS = a.logN - LOGR;
+  const long long Smask = (1LL << logS) - 1;
+  const int logNs = a.logNs;
+  const long long Nsmask = (1LL << logNs) - 1;
   const long long u0 = (long long)blockIdx.x * G;
   const int hmask = (1 << a.tw_h) - 1;
-  for (int lt = threadIdx.x; lt < R * G; lt += NT) {
+  const bool g_fast_in = logS >= 0 && (1LL << logS) >= G;
+  V vbuf[ITER];
+#pragma unroll
+  for (int q = 0; q < ITER; q++) {
+    const int lt = threadIdx.x + q * NT;
     int g, r;
-    if (S >= G) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+    if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
     const long long u = u0 + g;
-    const long long b = u / S, j = u - b * S;
-    const long long m = j + (long long)r * S;
+    const long long b = u >> logS, j = u & Smask;
+    const long long m = j + ((long long)r << logS);
     V v;
     if (u >= a.total) v = mk((T)0, (T)0);
     else if (gx) v = gx[a.goffs[b] + m * a.gstride];
     else v = in[b * a.bstride + m];
+    vbuf[q] = v;
+  }
+#pragma unroll
+  for (int q = 0; q < ITER; q++) {
+    const int lt = threadIdx.x + q * NT;
+    int g, r;
+    if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+    V v = vbuf[q];
     if (a.inverse) v.y = -v.y;
-    if (a.Ns > 1) {
-      const long long mm = (j % a.Ns) * r;  // < Ns * R
+    if (logNs > 0) {
+      const long long j = (u0 + g) & Smask;
+      const long long mm = (j & Nsmask) * r;  // < Ns * R
       V w = cmul(thi[mm >> a.tw_h], tlo[mm & hmask]);
       v = cmul(v, w);
     }
@@ -218,17 +238,20 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   cta_fft<V, LOGR, G>(sm, reinterpret_cast<const V *>(a.twR));
   V *__restrict__ out = reinterpret_cast<V *>(a.out);
   T *__restrict__ smp = reinterpret_cast<T *>(a.samples);
-  // R * G is a multiple of NT, so every warp runs the same trip count and
-  // its 32 lanes always hold elements of one batch row (R >= 128 > 32)
-  for (int lt = threadIdx.x; lt < R * G; lt += NT) {
+  const bool g_fast_out = logNs >= 0 && (1 << logNs) >= G;
+  // every warp runs the same trip count and its 32 lanes always hold elements
+  // of one batch row (R >= 128 > 32)
+#pragma unroll 4
+  for (int q = 0; q < ITER; q++) {
+    const int lt = threadIdx.x + q * NT;
     int g, k;
-    if (a.Ns >= G) { g = lt % G; k = lt / G; } else { k = lt % R; g = lt / R; }
+    if (g_fast_out) { g = lt % G; k = lt / G; } else { k = lt % R; g = lt / R; }
     const long long u = u0 + g;
     const bool live = u < a.total;
-    const long long b = u / S, j = u - b * S;
+    const long long b = u >> logS, j = u & Smask;
     T sv = 0;
     if (live) {
-      const long long dest = (j / a.Ns) * a.Ns * R + (j % a.Ns) + (long long)k * a.Ns;
+      const long long dest = ((j >> logNs) << (logNs + LOGR)) + (j & Nsmask) + ((long long)k << logNs);
       V v = sm[g * RP + padded(k)];
       if (a.inverse) v.y = -v.y;
       if (a.write_complex) out[b * a.bstride + dest] = v;
@@ -393,6 +416,12 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
     a.in = src;
     a.out = dst;
     a.N = p.n;
+    a.logN = p.L;
+    {
+      int l = 0;
+      while ((1LL << l) < Ns) l++;
+      a.logNs = l;
+    }
     a.bstride = p.n;
     a.batch = batch;
     a.Ns = (int)Ns;

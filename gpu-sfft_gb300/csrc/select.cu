@@ -142,13 +142,22 @@ sel_hist_kernel(const void *keys, long long row_stride, SelState *st, unsigned *
   __syncthreads();
   const long long base = (long long)blockIdx.x * SEL_TILE;
   const void *row = reinterpret_cast<const char *>(keys) + (size_t)b * row_stride * sizeof(K);
+  const int lane = threadIdx.x & 31;
 #pragma unroll 4
   for (int it = 0; it < SEL_ITEMS; it++) {
     const long long i = base + it * SEL_THREADS + threadIdx.x;
+    bool hit = false;
+    unsigned digit = 0;
     if (i < size) {
       const unsigned long long k = (unsigned long long)load_key<K>(row, i, floor);
-      if ((k & hi_mask) == prefix) atomicAdd(&sh[(unsigned)(k >> shift) & dmask], 1u);
+      hit = (k & hi_mask) == prefix;
+      digit = (unsigned)(k >> shift) & dmask;
     }
+    // warp-aggregated increment: lanes with the same digit add once
+    // (invalid lanes get distinct keys above the digit range)
+    const unsigned key = hit ? digit : (0x80000000u | (unsigned)lane);
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (hit && lane == __ffs(peers) - 1) atomicAdd(&sh[digit], (unsigned)__popc(peers));
   }
   __syncthreads();
   unsigned *gh = hist + (size_t)b * HIST_BINS;

@@ -51,6 +51,8 @@ int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
                      unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
                      cudaStream_t st);
 int vote_launches_per_loop();
+// ints needed by the blk scratch of launch_vote_loop
+int vote_block_ints(int B_thresh);
 
 // A8: estimates + |value|^2 keys for the candidates.
 int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, const void *bins,

@@ -145,73 +145,157 @@ __device__ __forceinline__ int window_low(int J, int n, int nb) {
   return (int)((c + n) & (long long)(n - 1));
 }
 
+// One warp per heavy bucket.  The window [low, low + n/B) is cut into chunks;
+// in chunk c lane L holds a 32-bit mask of visited positions (window offsets
+// 1024c + 32L .. +31 when the window is 32-aligned, else the single offset
+// 32c + L).  Chunks, lanes and bits in ascending order give the window in
+// ascending order.  chunk_fn(mask, pos_of_bit) is called once per chunk by
+// every lane (warp-uniform trip count).
+struct ChunkPos {
+  int r0, base, key, W, n, aligned;
+  // position of bit t of this lane's mask
+  __device__ __forceinline__ int operator()(int t) const {
+    const int rr = aligned ? r0 + t : r0;
+    const int blk = (rr >= key) ? base : ((base + W) & (n - 1));
+    return blk + rr;
+  }
+};
+
 template <class F>
-__device__ __forceinline__ void walk_window(const WalkArgs &w, int J, F &&visit) {
+__device__ __forceinline__ void for_each_chunk(const WalkArgs &w, int J, F &&chunk_fn) {
+  const int lane = threadIdx.x & 31;
   const int low = window_low(J, w.n, w.nb);
   const int key = low & (w.W - 1);
   if (key > *w.fmax) return;  // reference clamp: nothing visited
   const int base = low - key;
-  int pos = 0;
-  while (pos < w.nb) {
-    const int r = key + pos;
-    int rr = r, blk = base;
-    if (r >= w.W) { rr = r - w.W; blk = (base + w.W) & (w.n - 1); }
-    const int bit = rr & 31;
-    const int take = min(32 - bit, w.nb - pos);
-    unsigned word = __ldg(&w.bm[rr >> 5]) >> bit;
-    if (take < 32) word &= (1u << take) - 1u;
-    while (word) {
-      const int t = __ffs(word) - 1;
-      word &= word - 1;
-      visit(blk + rr + t);
+  const int aligned = ((key & 31) == 0 && (w.nb & 31) == 0) ? 1 : 0;
+  const int span = aligned ? 1024 : 32;
+  for (int c0 = 0; c0 < w.nb; c0 += span) {
+    unsigned mask = 0;
+    int r0 = 0;
+    if (aligned) {
+      const int off = c0 + lane * 32;
+      if (off < w.nb) {
+        r0 = key + off;
+        if (r0 >= w.W) r0 -= w.W;  // aligned words never straddle W
+        mask = __ldg(&w.bm[r0 >> 5]);
+      }
+    } else {
+      const int off = c0 + lane;
+      if (off < w.nb) {
+        int r = key + off;
+        if (r >= w.W) r -= w.W;
+        r0 = r;
+        mask = (__ldg(&w.bm[r >> 5]) >> (r & 31)) & 1u;
+      }
     }
-    pos += take;
+    ChunkPos pos{r0, base, key, w.W, w.n, aligned};
+    chunk_fn(mask, pos);
   }
 }
 
+__device__ __forceinline__ unsigned warp_excl_scan(unsigned v, unsigned *total) {
+  const int lane = threadIdx.x & 31;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  *total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
+}
+
+constexpr int WPB = VT / 32;  // buckets (warps) per block
+
 __global__ void __launch_bounds__(VT)
-vote_count_kernel(WalkArgs w, unsigned epoch, unsigned thresh, unsigned *vote, int *cnt, int *blk) {
+vote_count_kernel(WalkArgs w, unsigned epoch, unsigned thresh, unsigned *vote, int *cnt, int *blk,
+                  int *blk_pre, RunCtl *ctl) {
   __shared__ unsigned ws[VT / 32];
-  const int t = blockIdx.x * VT + threadIdx.x;
+  __shared__ int is_last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * WPB + warp;
   unsigned c = 0;
   if (t < w.Bt) {
     const unsigned nmask = (unsigned)w.n - 1u;
-    walk_window(w, w.J[t], [&](int p) {
-      const unsigned loc = ((unsigned)p * w.a) & nmask;
-      const unsigned e = vote[loc];
-      const unsigned cv = ((e >> 8) == epoch) ? (e & 255u) + 1u : 1u;
-      vote[loc] = (epoch << 8) | cv;
-      c += (cv == thresh);
+    for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
+      while (mask) {
+        const int b = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const unsigned loc = ((unsigned)pos(b) * w.a) & nmask;
+        const unsigned e = vote[loc];
+        const unsigned cv = ((e >> 8) == epoch) ? (e & 255u) + 1u : 1u;
+        vote[loc] = (epoch << 8) | cv;
+        c += (cv == thresh);
+      }
     });
-    cnt[t] = (int)c;
   }
-  const unsigned s = blk_sum(c, ws);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0 && t < w.Bt) cnt[t] = (int)c;
+  const unsigned s = blk_sum(lane == 0 ? c : 0u, ws);
   if (threadIdx.x == 0) blk[blockIdx.x] = (int)s;
+  // last block: exclusive scan of the block counts
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned tk = atomicAdd(&ctl->ticket, 1u);
+    is_last = tk == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  unsigned run = 0;
+  for (int c0 = 0; c0 < (int)gridDim.x; c0 += VT) {
+    const int i = c0 + threadIdx.x;
+    const unsigned v = i < (int)gridDim.x ? (unsigned)atomicAdd(&blk[i], 0) : 0u;
+    unsigned tot;
+    const unsigned e = blk_excl_scan(v, ws, &tot);
+    if (i < (int)gridDim.x) blk_pre[i] = (int)(run + e);
+    run += tot;
+  }
+  if (threadIdx.x == 0) {
+    blk_pre[gridDim.x] = (int)run;
+    ctl->ticket = 0;
+  }
 }
 
 __global__ void __launch_bounds__(VT)
 vote_write_kernel(WalkArgs w, unsigned epoch, unsigned thresh, const unsigned *__restrict__ vote,
-                  const int *__restrict__ cnt, const int *__restrict__ blk, int *cand, int cap,
-                  RunCtl *ctl) {
+                  const int *__restrict__ cnt, const int *__restrict__ blk_pre, int nblk, int *cand,
+                  int cap, RunCtl *ctl) {
   __shared__ unsigned ws[VT / 32];
   __shared__ int is_last;
   const int base_prev = ctl->cand_count;
-  unsigned before = 0;
-  for (int b = threadIdx.x; b < (int)blockIdx.x; b += VT) before += (unsigned)blk[b];
-  before = blk_sum(before, ws);
-  const int t = blockIdx.x * VT + threadIdx.x;
-  const unsigned c = t < w.Bt ? (unsigned)cnt[t] : 0u;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * WPB + warp;
+  const unsigned c = (t < w.Bt && lane == 0) ? (unsigned)cnt[t] : 0u;
   unsigned tot;
-  long long pos = (long long)base_prev + before + blk_excl_scan(c, ws, &tot);
-  if (c) {
+  const unsigned wpre = blk_excl_scan(c, ws, &tot);  // lane 0 of each warp carries its count
+  long long next = (long long)base_prev + blk_pre[blockIdx.x] + __shfl_sync(0xffffffffu, wpre, 0);
+  const unsigned cw = __shfl_sync(0xffffffffu, c, 0);
+  if (cw) {
     const unsigned nmask = (unsigned)w.n - 1u;
     const unsigned want = (epoch << 8) | thresh;
-    walk_window(w, w.J[t], [&](int p) {
-      const unsigned loc = ((unsigned)p * w.a) & nmask;
-      if (vote[loc] == want) {
-        if (pos < cap) cand[pos] = (int)loc;
-        pos++;
+    for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
+      // appended positions of this lane, in bit order
+      unsigned app = 0;
+      unsigned m = mask;
+      while (m) {
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        const unsigned loc = ((unsigned)pos(b) * w.a) & nmask;
+        if (vote[loc] == want) app |= 1u << b;
       }
+      unsigned ctot;
+      long long o = next + warp_excl_scan((unsigned)__popc(app), &ctot);
+      while (app) {
+        const int b = __ffs(app) - 1;
+        app &= app - 1;
+        if (o < cap) cand[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
+        o++;
+      }
+      next += ctot;
     });
   }
   __threadfence();
@@ -223,9 +307,7 @@ vote_write_kernel(WalkArgs w, unsigned epoch, unsigned thresh, const unsigned *_
   __syncthreads();
   if (is_last && threadIdx.x == 0) {
     __threadfence();
-    long long total = 0;
-    for (int b = 0; b < (int)gridDim.x; b++) total += blk[b];
-    const long long nc = (long long)base_prev + total;
+    const long long nc = (long long)base_prev + blk_pre[nblk];
     ctl->cand_count = (int)(nc > 0x7fffffffLL ? 0x7fffffffLL : nc);
     if (nc > cap) ctl->overflow = 1;
     ctl->ticket = 0;
@@ -276,13 +358,17 @@ int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
   w.bm = bitmap_l;
   w.fmax = &ctl->fmax[l];
   w.a = (unsigned)d.a[l];
-  const int grid = (B_thresh + VT - 1) / VT;
-  vote_count_kernel<<<grid, VT, 0, st>>>(w, epoch, (unsigned)loops_thresh, vote, cnt, blk);
-  GS_LAUNCHED();
-  vote_write_kernel<<<grid, VT, 0, st>>>(w, epoch, (unsigned)loops_thresh, vote, cnt, blk, cand, cap,
+  const int grid = (B_thresh + WPB - 1) / WPB;
+  int *blk_pre = blk + grid + 1;  // blk holds 2 * (grid + 1) ints
+  vote_count_kernel<<<grid, VT, 0, st>>>(w, epoch, (unsigned)loops_thresh, vote, cnt, blk, blk_pre,
                                          ctl);
+  GS_LAUNCHED();
+  vote_write_kernel<<<grid, VT, 0, st>>>(w, epoch, (unsigned)loops_thresh, vote, cnt, blk_pre, grid,
+                                         cand, cap, ctl);
   GS_LAUNCHED();
   return GSFFT_OK;
 }
+
+int vote_block_ints(int B_thresh) { return 2 * ((B_thresh + WPB - 1) / WPB + 1); }
 
 }  // namespace gsfft
