@@ -241,6 +241,29 @@ int gsfft_stage_perm_filter(int precision, const void *d_x, int n, const complex
   return s;
 }
 
+int gsfft_stage_perm_filter_stream(int precision, const void *d_x, int n,
+                                   const complex_t *d_filter_time, int w, int B, int loops,
+                                   const int *h_a, void *d_bins, void *stream) {
+  if (!d_x || !d_filter_time || !d_bins || !h_a || loops < 2 || loops > 16) return GSFFT_ERR_PARAM;
+  if (n < 2 || (n & (n - 1)) || B < 1 || (B & (B - 1)) || B > n / 2 || w < 1 || w > n)
+    return GSFFT_ERR_PARAM;
+  if (!stream_pf_supported(n, B, loops, n, 0)) return GSFFT_ERR_UNSUPPORTED;
+  Draws d;
+  memset(&d, 0, sizeof(d));
+  for (int l = 0; l < loops; l++) d.a[l] = h_a[l];
+  const bool fl = precision == GSFFT_MIXED;
+  void *taps = nullptr;
+  if (fl && cudaMalloc(&taps, sizeof(float2) * (size_t)w) != cudaSuccess) return GSFFT_ERR_ALLOC;
+  int s = GSFFT_OK;
+  if (fl) s = launch_convert_taps((const double2 *)d_filter_time, taps, w, true, S(stream));
+  if (s == GSFFT_OK)
+    s = launch_perm_filter_stream(precision, d_x, n, fl ? taps : (const void *)d_filter_time, w, B,
+                                  loops, d, d_bins, 0, nullptr, n, S(stream));
+  if (s == GSFFT_OK) s = sync_check(S(stream), "gsfft_stage_perm_filter_stream");
+  if (taps) cudaFree(taps);
+  return s;
+}
+
 int gsfft_stage_reverse_hash(const int *d_J, int B_thresh, const int *d_J2, int num_RLFC, int n,
                              int B, int W_RLFC, int a, int ai, int loops_thresh, unsigned epoch,
                              unsigned *d_vote, int *d_cand, int cap, int *h_count, void *stream) {

@@ -107,6 +107,18 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   A(topk, sizeof(DevNode) * (size_t)p.k + 16);
   A(ctl, sizeof(RunCtl));
   A(rmax, sizeof(unsigned long long) * (size_t)(p.RLFC_loops + p.loops));
+  // perm+filter form: one ordered pass over x when that moves fewer DRAM bytes
+  // than loops*w + RLFC_loops*W random reads (~80 bytes per random read)
+  {
+    const double stream_bytes = (double)p.n * V + 2.0 * p.RLFC_loops * p.W_RLFC * V;
+    const double gather_bytes = 80.0 * ((double)p.loops * p.w + (double)p.RLFC_loops * p.W_RLFC);
+    const bool ok = stream_pf_supported(p.n, p.B, p.loops, p.W_RLFC, p.RLFC_loops) &&
+                    !(flags & GSFFT_FLAG_QUIRK_RESIDUE);
+    P->use_stream = ok && !(flags & GSFFT_FLAG_FORCE_GATHER) &&
+                    ((flags & GSFFT_FLAG_FORCE_STREAM) ||
+                     (precision == GSFFT_MIXED && stream_bytes < gather_bytes));
+  }
+  if (P->use_stream) A(ybuf, V * (size_t)p.RLFC_loops * p.W_RLFC);
 #undef A
   P->floor_rel = (flags & GSFFT_FLAG_RAW_SELECTION) ? 0.0 : 1e-10;
   if (s == GSFFT_OK) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
@@ -136,7 +148,7 @@ void plan_destroy(Plan *P) {
   if (!P) return;
   void *ptrs[] = {P->filt, P->hinv, P->rsamp, P->J2b, P->J2, P->bins, P->bsamp, P->J,
                   P->bm_j2, P->bm_sig, P->tile_tmp, P->vote, P->cand, P->cnt, P->blk,
-                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax};
+                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax, P->ybuf};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
@@ -184,6 +196,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   for (int l = 0; l < p.loops; l++) {
     if ((a[l] & 1) == 0 || (ai[l] & 1) == 0 || a[l] <= 0 || ai[l] <= 0 || a[l] >= p.n || ai[l] >= p.n)
       return GSFFT_ERR_PARAM;
+    if ((unsigned)a[l] * (unsigned)ai[l] % (unsigned)p.n != 1u) return GSFFT_ERR_PARAM;
     d.a[l] = a[l];
     d.ai[l] = ai[l];
   }
@@ -196,74 +209,98 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   GS_CUDA(cudaMemsetAsync(P->ctl, 0, sizeof(RunCtl), st));
   const int kb = P->precision == GSFFT_FP64 ? 8 : 4;
   GS_CUDA(cudaMemsetAsync(P->rmax, 0, sizeof(unsigned long long) * (p.RLFC_loops + p.loops), st));
-  // row maxima as u64 (FP64) or u32 (FP32) arrays
-  void *rmax_w = P->rmax;
+  void *rmax_w = P->rmax;  // RLFC rows, then bucket rows (u64 in FP64, u32 in FP32)
   void *rmax_b = (char *)P->rmax + (size_t)kb * p.RLFC_loops;
   cudaEvent_t *ev = nullptr;
   if (P->timing && P->timed_runs < 512) {
-    const size_t need = (size_t)(P->timed_runs + 1) * (ST_COUNT + 1);
+    const size_t need = (size_t)(P->timed_runs + 1) * (2 * ST_COUNT);
     while (P->events.size() < need) {
       cudaEvent_t e;
       GS_CUDA(cudaEventCreate(&e));
       P->events.push_back(e);
     }
-    ev = &P->events[(size_t)P->timed_runs * (ST_COUNT + 1)];
+    ev = &P->events[(size_t)P->timed_runs * (2 * ST_COUNT)];
     P->timed_runs++;
   }
-#define MARK(i) \
-  if (ev) GS_CUDA(cudaEventRecord(ev[i], st))
-  MARK(0);
+#define BEGIN(s) \
+  if (ev) GS_CUDA(cudaEventRecord(ev[2 * (s)], st))
+#define END(s) \
+  if (ev) GS_CUDA(cudaEventRecord(ev[2 * (s) + 1], st))
+  const bool quirk = (P->flags & GSFFT_FLAG_QUIRK_RESIDUE) != 0;
 
-  // A4: RLFC -- strided gather fused into the first FFT pass, |.|^2 epilogue
+  // A5 (+ RLFC sub-sampling when streaming): bins of every loop
+  BEGIN(ST_PERM_FILTER);
+  if (P->use_stream)
+    GS_CHECK(launch_perm_filter_stream(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d,
+                                       P->bins, p.RLFC_loops, P->ybuf, p.W_RLFC, st));
+  else
+    GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d, quirk,
+                                P->bins, st));
+  END(ST_PERM_FILTER);
+
+  // A4: RLFC -- W-point FFT of the sub-sampled signal, |.|^2 epilogue, cutoff
+  BEGIN(ST_RLFC_FFT);
   {
     FftIo io;
-    io.gather_x = d_x;
-    for (int r = 0; r < p.RLFC_loops; r++) io.gather_offsets[r] = d.offs[r];
-    io.gather_stride = p.n / p.W_RLFC;
+    const void *src = nullptr;
+    if (P->use_stream) {
+      src = P->ybuf;
+    } else {
+      io.gather_x = d_x;  // strided gather fused into the first FFT pass
+      for (int r = 0; r < p.RLFC_loops; r++) io.gather_offsets[r] = d.offs[r];
+      io.gather_stride = p.n / p.W_RLFC;
+    }
     io.samples = P->rsamp;
     io.row_max = rmax_w;
     io.write_complex = false;
-    GS_CHECK(fft_exec(P->fftW, nullptr, P->rsamp, p.RLFC_loops, -1, io, st));
-    MARK(1);
-    GS_CHECK(select_top(P->rsamp, kb, p.W_RLFC, nullptr, p.B_thresh, p.RLFC_loops, p.W_RLFC,
-                        P->J2b, p.B_thresh, nullptr, P->selW, st, rmax_w, P->floor_rel));
-    MARK(2);
-    GS_CHECK(launch_j2_merge(P->J2b, p.RLFC_loops * p.B_thresh, p.W_RLFC, P->bm_j2, P->J2, P->ctl,
-                             P->tile_tmp, st));
-    GS_CHECK(launch_sigma_bitmaps(P->J2, P->ctl, p.RLFC_loops * p.B_thresh, p.W_RLFC,
-                                  p.loops_loc, d, P->bm_sig, P->ctl, st));
+    GS_CHECK(fft_exec(P->fftW, src, P->rsamp, p.RLFC_loops, -1, io, st));
   }
-  MARK(3);
-  // A5 + A6: perm+filter for every loop, bucket FFT, cutoff of location loops
-  GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d,
-                              (P->flags & GSFFT_FLAG_QUIRK_RESIDUE) != 0, P->bins, st));
-  MARK(4);
+  END(ST_RLFC_FFT);
+  BEGIN(ST_RLFC_SELECT);
+  GS_CHECK(select_top(P->rsamp, kb, p.W_RLFC, nullptr, p.B_thresh, p.RLFC_loops, p.W_RLFC, P->J2b,
+                      p.B_thresh, nullptr, P->selW, st, rmax_w, P->floor_rel));
+  END(ST_RLFC_SELECT);
+  BEGIN(ST_J2);
+  GS_CHECK(launch_j2_merge(P->J2b, p.RLFC_loops * p.B_thresh, p.W_RLFC, P->bm_j2, P->J2, P->ctl,
+                           P->tile_tmp, st));
+  GS_CHECK(launch_sigma_bitmaps(P->J2, P->ctl, p.RLFC_loops * p.B_thresh, p.W_RLFC, p.loops_loc, d,
+                                P->bm_sig, P->ctl, st));
+  END(ST_J2);
+
+  // A6: bucket FFT of every loop, cutoff of the location loops
+  BEGIN(ST_BUCKET_FFT);
   {
     FftIo io;
     io.samples = P->bsamp;
     io.row_max = rmax_b;
     GS_CHECK(fft_exec(P->fftB, P->bins, P->bins, p.loops, -1, io, st));
   }
-  MARK(5);
+  END(ST_BUCKET_FFT);
+  BEGIN(ST_CUTOFF);
   GS_CHECK(select_top(P->bsamp, kb, p.B, nullptr, p.B_thresh, p.loops_loc, p.B, P->J, p.B_thresh,
                       nullptr, P->selB, st, rmax_b, P->floor_rel));
-  MARK(6);
+  END(ST_CUTOFF);
+
   // A7: voting, one location loop after the other
+  BEGIN(ST_VOTE);
   const size_t wW = (size_t)p.W_RLFC / 32;
   for (int l = 0; l < p.loops_loc; l++)
     GS_CHECK(launch_vote_loop(l, P->J + (size_t)l * p.B_thresh, p.B_thresh, p.n, p.B, p.W_RLFC,
                               P->bm_sig + wW * l, d, p.loops_thresh, P->epoch, P->vote, P->cand,
                               P->cap, P->cnt, P->blk, P->ctl, st));
-  MARK(7);
+  END(ST_VOTE);
   // A8: estimation; A9: k largest
+  BEGIN(ST_ESTIMATE);
   GS_CHECK(launch_estimate(P->precision, P->cand, P->ctl, P->cap, P->bins, p.loops, p.n, p.B, d,
                            P->hinv, P->nodes, P->mag2, st));
-  MARK(8);
+  END(ST_ESTIMATE);
+  BEGIN(ST_TOPK);
   GS_CHECK(select_top(P->mag2, 8, P->cap, &P->ctl->cand_count, p.k, 1, P->cap, P->topk_idx, p.k,
                       &P->ctl->n_topk, P->selK, st));
   GS_CHECK(launch_gather_nodes(P->nodes, P->topk_idx, &P->ctl->n_topk, p.k, P->topk, st));
-  MARK(9);
-#undef MARK
+  END(ST_TOPK);
+#undef BEGIN
+#undef END
   P->launches_per_run = g_launch_counter - before;
   P->ran = true;
   return GSFFT_OK;
@@ -279,13 +316,16 @@ int plan_results(Plan *P, Node *h_nodes, int nodes_cap, int *I_F, Node *h_topk, 
   if (I_F) *I_F = c.cand_count;
   if (h_nodes && nodes_cap > 0) {
     const int m = count < nodes_cap ? count : nodes_cap;
-    if (m > 0) GS_CUDA(cudaMemcpy(h_nodes, P->nodes, sizeof(Node) * m, cudaMemcpyDeviceToHost));
+    if (m > 0)
+      GS_CUDA(cudaMemcpyAsync(h_nodes, P->nodes, sizeof(Node) * m, cudaMemcpyDeviceToHost, st));
   }
   if (n_topk) *n_topk = c.n_topk;
   if (h_topk && topk_cap > 0) {
     const int m = c.n_topk < topk_cap ? c.n_topk : topk_cap;
-    if (m > 0) GS_CUDA(cudaMemcpy(h_topk, P->topk, sizeof(Node) * m, cudaMemcpyDeviceToHost));
+    if (m > 0)
+      GS_CUDA(cudaMemcpyAsync(h_topk, P->topk, sizeof(Node) * m, cudaMemcpyDeviceToHost, st));
   }
+  GS_CUDA(cudaStreamSynchronize(st));
   return c.overflow ? GSFFT_ERR_CAPACITY : GSFFT_OK;
 }
 
@@ -309,8 +349,8 @@ int plan_stage_times(Plan *P, float *ms_avg, int max_stages, int *runs) {
     double acc = 0.0;
     for (int r = 0; r < R; r++) {
       float ms = 0.f;
-      cudaEvent_t *e = &P->events[(size_t)r * (ST_COUNT + 1)];
-      GS_CUDA(cudaEventElapsedTime(&ms, e[sidx], e[sidx + 1]));
+      cudaEvent_t *e = &P->events[(size_t)r * (2 * ST_COUNT)];
+      GS_CUDA(cudaEventElapsedTime(&ms, e[2 * sidx], e[2 * sidx + 1]));
       acc += ms;
     }
     ms_avg[sidx] = R ? (float)(acc / R) : 0.f;

@@ -38,10 +38,12 @@ struct Plan {
   DevNode *topk = nullptr;
   RunCtl *ctl = nullptr;
   void *rmax = nullptr;  // per-row maxima: RLFC_loops rows then loops rows (u64 each)
+  void *ybuf = nullptr;  // RLFC sub-samples written by the streaming perm+filter
+  bool use_stream = false;
   double floor_rel = 1e-10;
   // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
   bool timing = false;
-  std::vector<cudaEvent_t> events;  // (ST_COUNT + 1) per recorded run
+  std::vector<cudaEvent_t> events;  // 2 * ST_COUNT per recorded run (begin, end)
   int timed_runs = 0;
 };
 

@@ -83,6 +83,15 @@ template <> __host__ __device__ constexpr int g_of<float>(int logr) {
 template <typename T> __host__ __device__ constexpr int nt_of(int logr) {
   return imin(((1 << logr) / 16) * g_of<T>(logr), 512);
 }
+// Resident CTAs per SM the register budget is sized for, so that the loads,
+// shared-memory butterflies and stores of different CTAs overlap.  A thread
+// holds one radix-16 butterfly when (R/16)*G <= 512 (Q = 1); then FP32 fits
+// 64 registers (two 512-thread CTAs) and FP64 128 (two 256-thread CTAs).
+template <typename T> __host__ __device__ constexpr int minb_of(int logr) {
+  return ((1 << logr) / 16) * g_of<T>(logr) > 512
+             ? 1
+             : (sizeof(T) == 4 ? (nt_of<T>(logr) >= 512 ? 2 : 4) : (nt_of<T>(logr) >= 512 ? 1 : 2));
+}
 __host__ __device__ constexpr int padded(int i) { return i + (i >> 4); }
 template <typename T> __host__ __device__ constexpr int smem_of(int logr) {
   return g_of<T>(logr) * padded(1 << logr) * (int)sizeof(typename Cx<T>::V);
@@ -186,7 +195,7 @@ __device__ __forceinline__ void row_max_update(void *rm, long long b, float v) {
 }
 
 template <typename T, int LOGR>
-__global__ void __launch_bounds__(nt_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
+__global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   typedef typename Cx<T>::V V;
   constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = padded(R);
   constexpr int ITER = R * G / NT;  // elements per thread in the load / store phases
@@ -204,35 +213,39 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   const long long u0 = (long long)blockIdx.x * G;
   const int hmask = (1 << a.tw_h) - 1;
   const bool g_fast_in = logS >= 0 && (1LL << logS) >= G;
-  V vbuf[ITER];
+  constexpr int LB = ITER < 4 ? ITER : 4;  // loads in flight per thread
 #pragma unroll
-  for (int q = 0; q < ITER; q++) {
-    const int lt = threadIdx.x + q * NT;
-    int g, r;
-    if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
-    const long long u = u0 + g;
-    const long long b = u >> logS, j = u & Smask;
-    const long long m = j + ((long long)r << logS);
-    V v;
-    if (u >= a.total) v = mk((T)0, (T)0);
-    else if (gx) v = gx[a.goffs[b] + m * a.gstride];
-    else v = in[b * a.bstride + m];
-    vbuf[q] = v;
-  }
+  for (int q0 = 0; q0 < ITER; q0 += LB) {
+    V vbuf[LB];
 #pragma unroll
-  for (int q = 0; q < ITER; q++) {
-    const int lt = threadIdx.x + q * NT;
-    int g, r;
-    if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
-    V v = vbuf[q];
-    if (a.inverse) v.y = -v.y;
-    if (logNs > 0) {
-      const long long j = (u0 + g) & Smask;
-      const long long mm = (j & Nsmask) * r;  // < Ns * R
-      V w = cmul(thi[mm >> a.tw_h], tlo[mm & hmask]);
-      v = cmul(v, w);
+    for (int q = 0; q < LB; q++) {
+      const int lt = threadIdx.x + (q0 + q) * NT;
+      int g, r;
+      if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+      const long long u = u0 + g;
+      const long long b = u >> logS, j = u & Smask;
+      const long long m = j + ((long long)r << logS);
+      V v;
+      if (u >= a.total) v = mk((T)0, (T)0);
+      else if (gx) v = gx[a.goffs[b] + m * a.gstride];
+      else v = in[b * a.bstride + m];
+      vbuf[q] = v;
     }
-    sm[g * RP + padded(r)] = v;
+#pragma unroll
+    for (int q = 0; q < LB; q++) {
+      const int lt = threadIdx.x + (q0 + q) * NT;
+      int g, r;
+      if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+      V v = vbuf[q];
+      if (a.inverse) v.y = -v.y;
+      if (logNs > 0) {
+        const long long j = (u0 + g) & Smask;
+        const long long mm = (j & Nsmask) * r;  // < Ns * R
+        V w = cmul(thi[mm >> a.tw_h], tlo[mm & hmask]);
+        v = cmul(v, w);
+      }
+      sm[g * RP + padded(r)] = v;
+    }
   }
   __syncthreads();
   cta_fft<V, LOGR, G>(sm, reinterpret_cast<const V *>(a.twR));

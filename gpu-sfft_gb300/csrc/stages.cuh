@@ -35,6 +35,13 @@ struct DevNode {  // == Node (utils.h:42-45)
 int launch_perm_filter(int precision, const void *x, int n, const void *filt, int w, int B,
                        int loops, const Draws &d, bool quirk_residue, void *bins, cudaStream_t st);
 
+// A5 (and the RLFC sub-sampling) as one ordered pass over x; y receives
+// RLFC_loops rows of W samples (x[off_r + m*n/W]).  FP64 or FP32.
+bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops);
+int launch_perm_filter_stream(int precision, const void *x, int n, const void *filt, int w, int B,
+                              int loops, const Draws &d, void *bins, int nrlfc, void *y, int W,
+                              cudaStream_t st);
+
 // J2 = sorted distinct union of the RLFC blocks, through a W-bit bitmap.
 int launch_j2_merge(const int *J2_blocks, int total, int W, unsigned *bitmap, int *J2,
                     RunCtl *ctl, unsigned *tile_tmp, cudaStream_t st);

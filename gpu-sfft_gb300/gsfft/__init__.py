@@ -22,6 +22,8 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "gsfft.h")
 FP64, MIXED = 0, 1
 FLAG_QUIRK_RESIDUE = 1
 FLAG_RAW_SELECTION = 2
+FLAG_FORCE_GATHER = 4
+FLAG_FORCE_STREAM = 8
 SELECTION_FLOOR = 1e-10
 OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE = range(7)
 
@@ -86,6 +88,7 @@ def lib():
         "gsfft_fft": ([P, P, ll, i, i, i, P], i),
         "gsfft_cutoff": ([P, i, i, i, i, P, P], i),
         "gsfft_stage_perm_filter": ([i, P, i, P, i, i, i, P, i, P, P], i),
+        "gsfft_stage_perm_filter_stream": ([i, P, i, P, i, i, i, P, P, P], i),
         "gsfft_stage_reverse_hash": ([P, i, P, i, i, i, i, i, i, i, u, P, P, i,
                                       C.POINTER(i), P], i),
         "gsfft_stage_estimate": ([i, P, i, P, i, i, i, P, P, P, P], i),
@@ -158,6 +161,13 @@ def stage_perm_filter(precision, d_x, n, d_filter_time, w, B, ai, d_bins, quirk_
     check(lib().gsfft_stage_perm_filter(precision, d_x, n, d_filter_time, w, B, ai.size,
                                         _np_ptr(ai), int(quirk_residue), d_bins, stream or None),
           "gsfft_stage_perm_filter")
+
+
+def stage_perm_filter_stream(precision, d_x, n, d_filter_time, w, B, a, d_bins, stream=0):
+    a = np.ascontiguousarray(a, np.int32)
+    check(lib().gsfft_stage_perm_filter_stream(precision, d_x, n, d_filter_time, w, B, a.size,
+                                               _np_ptr(a), d_bins, stream or None),
+          "gsfft_stage_perm_filter_stream")
 
 
 def stage_reverse_hash(d_J, B_thresh, d_J2, num_RLFC, n, B, W, a, ai, loops_thresh, epoch,

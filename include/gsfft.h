@@ -55,6 +55,11 @@ typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
    RLFC and bucket cutoffs, so that bins which are zero in exact arithmetic
    (half the RLFC picks of a noiseless signal) tie and resolve by ascending
    index, the reference's tie rule, instead of by FFT rounding noise. */
+#define GSFFT_FLAG_FORCE_GATHER 4u   /* perm+filter by random gathers (one read per
+   tap, innerLoop.cu:725-773 order) even when one ordered pass over the signal
+   would move fewer DRAM bytes */
+#define GSFFT_FLAG_FORCE_STREAM 8u   /* perm+filter (and the RLFC sub-sampling) by
+   one ordered pass over the signal whenever the sizes allow it */
 
 /* Run parameters derived exactly as experiment.c:71-84 and
  * cuExperiment.cu:279-284 derive them. */
@@ -155,6 +160,11 @@ int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precis
 int gsfft_stage_perm_filter(int precision, const void *d_x, int n,
                             const complex_t *d_filter_time, int w, int B, int loops,
                             const int *h_ai, int quirk_residue, void *d_bins, void *stream);
+/* A5 as one ordered pass over x (same sums as gsfft_stage_perm_filter, taps
+ * of a bucket added in increasing signal position); h_a = sigma per loop. */
+int gsfft_stage_perm_filter_stream(int precision, const void *d_x, int n,
+                                   const complex_t *d_filter_time, int w, int B, int loops,
+                                   const int *h_a, void *d_bins, void *stream);
 /* A7 (reverse_hash, innerLoop.cu:300-384) for one location loop.  d_vote: n
  * entries, epoch << 8 | count (epoch 0 = plain counts, the reference's int
  * table).  Appends to d_cand from *h_count on; *h_count is updated (it may

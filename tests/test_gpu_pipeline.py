@@ -136,11 +136,29 @@ def test_fp64_residue_quirk(G, O, torch_cuda, name):
     assert recovered(g["topk"], loc) == recovered(O.topk(o["nodes"], p.k), loc)
 
 
-def test_deterministic_repeat(G, O, torch_cuda):
+@pytest.mark.parametrize("prec", [0, 1])
+def test_stream_and_gather_agree(G, O, torch_cuda, prec):
+    """Both perm+filter forms (and both RLFC sub-sampling paths) give the same
+    candidates; values agree to the precision's rounding."""
+    torch = torch_cuda
+    p, p_g, x, loc, X, ft, ff, draws = setup(G, O, torch, CFGS["config1"], seed=4)
+    gs = run_gpu(G, torch, p_g, x, ft, ff, draws, prec=prec, flags=G.FLAG_FORCE_STREAM)
+    gg = run_gpu(G, torch, p_g, x, ft, ff, draws, prec=prec, flags=G.FLAG_FORCE_GATHER)
+    np.testing.assert_array_equal(gs["stages"]["J2"], gg["stages"]["J2"])
+    np.testing.assert_array_equal(gs["nodes"]["key"], gg["nodes"]["key"])
+    vs = gs["nodes"]["x"] + 1j * gs["nodes"]["y"]
+    vg = gg["nodes"]["x"] + 1j * gg["nodes"]["y"]
+    tol = 1e-12 if prec == 0 else 1e-5
+    assert np.abs(vs - vg).max() <= tol * np.abs(vg).max()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_deterministic_repeat(G, O, torch_cuda, prec):
     torch = torch_cuda
     p, p_g, x, loc, X, ft, ff, draws = setup(G, O, torch, CFGS["config1"], seed=5)
-    plan = G.Plan(p_g, 0)
-    d_ft, d_ff, d_x = dev(torch, ft), dev(torch, ff), dev(torch, x)
+    plan = G.Plan(p_g, prec)
+    d_ft, d_ff = dev(torch, ft), dev(torch, ff)
+    d_x = dev(torch, x.astype(np.complex128 if prec == 0 else np.complex64))
     plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
     outs = []
     for _ in range(3):

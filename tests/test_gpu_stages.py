@@ -160,3 +160,28 @@ def test_estimate(G, O, torch_cuda, prec):
     scale = np.abs(ref["x"] + 1j * ref["y"]).max()
     assert np.abs(got["x"] - ref["x"]).max() <= 1e-13 * scale
     assert np.abs(got["y"] - ref["y"]).max() <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("n,B,w,loops", [(1 << 16, 256, 3479, 9), (1 << 20, 8192, 123349, 7),
+                                         (1 << 18, 1024, 200001, 2)])
+def test_perm_filter_stream(G, O, torch_cuda, prec, n, B, w, loops):
+    """The ordered pass over x computes the same bucket sums (taps of a bucket
+    added in increasing signal position instead of increasing tap index)."""
+    torch = torch_cuda
+    rng = np.random.default_rng(n + loops)
+    x = rng.normal(size=n) + 1j * rng.normal(size=n)
+    f = rng.normal(size=w) + 1j * rng.normal(size=w)
+    a = (rng.integers(0, n // 2, size=loops) * 2 + 1).astype(np.int64)
+    ai = np.array([pow(int(v), -1, n) for v in a])
+    dt = np.complex128 if prec == 0 else np.complex64
+    d_x, d_f = dev(torch, x.astype(dt)), dev(torch, f)
+    d_bins = torch.zeros((loops, B), dtype=torch.complex128 if prec == 0 else torch.complex64,
+                         device="cuda")
+    G.stage_perm_filter_stream(prec, d_x.data_ptr(), n, d_f.data_ptr(), w, B, a.astype(np.int32),
+                               d_bins.data_ptr())
+    got = d_bins.cpu().numpy()
+    tol = 1e-13 if prec == 0 else 1e-5
+    for l in range(loops):
+        ref = O.perm_filter(x, n, f, B, int(ai[l]))
+        assert np.abs(got[l] - ref).max() <= tol * np.abs(ref).max()
