@@ -247,20 +247,33 @@ int gsfft_stage_perm_filter_stream(int precision, const void *d_x, int n,
   if (!d_x || !d_filter_time || !d_bins || !h_a || loops < 2 || loops > 16) return GSFFT_ERR_PARAM;
   if (n < 2 || (n & (n - 1)) || B < 1 || (B & (B - 1)) || B > n / 2 || w < 1 || w > n)
     return GSFFT_ERR_PARAM;
-  if (!stream_pf_supported(n, B, loops, n, 0)) return GSFFT_ERR_UNSUPPORTED;
+  if (!stream_pf_supported(n, B, loops, n, 0) || w / B >= 32) return GSFFT_ERR_UNSUPPORTED;
   Draws d;
   memset(&d, 0, sizeof(d));
   for (int l = 0; l < loops; l++) d.a[l] = h_a[l];
   const bool fl = precision == GSFFT_MIXED;
   void *taps = nullptr;
-  if (fl && cudaMalloc(&taps, sizeof(float2) * (size_t)w) != cudaSuccess) return GSFFT_ERR_ALLOC;
-  int s = GSFFT_OK;
-  if (fl) s = launch_convert_taps((const double2 *)d_filter_time, taps, w, true, S(stream));
+  int *err = nullptr;
+  if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return GSFFT_ERR_ALLOC;
+  if (fl && cudaMalloc(&taps, sizeof(float2) * (size_t)w) != cudaSuccess) {
+    cudaFree(err);
+    return GSFFT_ERR_ALLOC;
+  }
+  int s = cudaMemsetAsync(err, 0, sizeof(int), S(stream)) == cudaSuccess ? GSFFT_OK : GSFFT_ERR_CUDA;
+  if (s == GSFFT_OK && fl) s = launch_convert_taps((const double2 *)d_filter_time, taps, w, true, S(stream));
   if (s == GSFFT_OK)
     s = launch_perm_filter_stream(precision, d_x, n, fl ? taps : (const void *)d_filter_time, w, B,
-                                  loops, d, d_bins, 0, nullptr, n, S(stream));
+                                  loops, d, d_bins, 0, nullptr, n, err, S(stream));
   if (s == GSFFT_OK) s = sync_check(S(stream), "gsfft_stage_perm_filter_stream");
+  int herr = 0;
+  if (s == GSFFT_OK && cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    s = GSFFT_ERR_CUDA;
+  if (s == GSFFT_OK && herr) {
+    set_last_error("a device-side wait timed out (streaming perm+filter)");
+    s = GSFFT_ERR_CUDA;
+  }
   if (taps) cudaFree(taps);
+  cudaFree(err);
   return s;
 }
 

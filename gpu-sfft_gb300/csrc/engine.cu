@@ -113,7 +113,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
     const double stream_bytes = (double)p.n * V + 2.0 * p.RLFC_loops * p.W_RLFC * V;
     const double gather_bytes = 80.0 * ((double)p.loops * p.w + (double)p.RLFC_loops * p.W_RLFC);
     const bool ok = stream_pf_supported(p.n, p.B, p.loops, p.W_RLFC, p.RLFC_loops) &&
-                    !(flags & GSFFT_FLAG_QUIRK_RESIDUE);
+                    p.w / p.B < 32 && !(flags & GSFFT_FLAG_QUIRK_RESIDUE);
     P->use_stream = ok && !(flags & GSFFT_FLAG_FORCE_GATHER) &&
                     ((flags & GSFFT_FLAG_FORCE_STREAM) ||
                      (precision == GSFFT_MIXED && stream_bytes < gather_bytes));
@@ -232,7 +232,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   BEGIN(ST_PERM_FILTER);
   if (P->use_stream)
     GS_CHECK(launch_perm_filter_stream(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d,
-                                       P->bins, p.RLFC_loops, P->ybuf, p.W_RLFC, st));
+                                       P->bins, p.RLFC_loops, P->ybuf, p.W_RLFC, &P->ctl->err, st));
   else
     GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d, quirk,
                                 P->bins, st));
@@ -326,6 +326,10 @@ int plan_results(Plan *P, Node *h_nodes, int nodes_cap, int *I_F, Node *h_topk, 
       GS_CUDA(cudaMemcpyAsync(h_topk, P->topk, sizeof(Node) * m, cudaMemcpyDeviceToHost, st));
   }
   GS_CUDA(cudaStreamSynchronize(st));
+  if (c.err) {
+    set_last_error("a device-side wait timed out (streaming perm+filter)");
+    return GSFFT_ERR_CUDA;
+  }
   return c.overflow ? GSFFT_ERR_CAPACITY : GSFFT_OK;
 }
 

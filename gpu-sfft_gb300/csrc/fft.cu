@@ -93,15 +93,25 @@ template <typename T> __host__ __device__ constexpr int minb_of(int logr) {
              : (sizeof(T) == 4 ? (nt_of<T>(logr) >= 512 ? 2 : 4) : (nt_of<T>(logr) >= 512 ? 1 : 2));
 }
 __host__ __device__ constexpr int padded(int i) { return i + (i >> 4); }
+// row stride in elements: one extra element so the G rows start in different banks
+__host__ __device__ constexpr int rowpitch(int logr) { return padded(1 << logr) + 1; }
+// twiddle table exp(-2 pi i m / R) copied into shared memory when it fits
+template <typename T> __host__ __device__ constexpr int data_smem_of(int logr) {
+  return g_of<T>(logr) * rowpitch(logr) * (int)sizeof(typename Cx<T>::V);
+}
+template <typename T> __host__ __device__ constexpr bool tw_in_smem(int logr) {
+  return data_smem_of<T>(logr) + (1 << logr) * (int)sizeof(typename Cx<T>::V) <= 220 * 1024;
+}
 template <typename T> __host__ __device__ constexpr int smem_of(int logr) {
-  return g_of<T>(logr) * padded(1 << logr) * (int)sizeof(typename Cx<T>::V);
+  return data_smem_of<T>(logr) +
+         (tw_in_smem<T>(logr) ? (1 << logr) * (int)sizeof(typename Cx<T>::V) : 0);
 }
 
 // One Stockham stage of radix E inside shared memory, for all G rows.
 template <typename V, int LOGR, int G, int E>
 __device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR, int Ns) {
   constexpr int R = 1 << LOGR;
-  constexpr int RP = padded(R);
+  constexpr int RP = rowpitch(LOGR);
   constexpr int NT = imin((R / 16) * G, 512);
   constexpr int TPF = NT / G;
   constexpr int NB = R / E;          // butterflies per row
@@ -197,10 +207,16 @@ __device__ __forceinline__ void row_max_update(void *rm, long long b, float v) {
 template <typename T, int LOGR>
 __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   typedef typename Cx<T>::V V;
-  constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = padded(R);
+  constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = rowpitch(LOGR);
   constexpr int ITER = R * G / NT;  // elements per thread in the load / store phases
   extern __shared__ __align__(16) unsigned char smraw[];
   V *sm = reinterpret_cast<V *>(smraw);
+  const V *twR = reinterpret_cast<const V *>(a.twR);
+  if (tw_in_smem<T>(LOGR)) {
+    V *tws = reinterpret_cast<V *>(smraw + data_smem_of<T>(LOGR));
+    for (int i = threadIdx.x; i < R; i += NT) tws[i] = twR[i];
+    twR = tws;  // made visible by the barrier before the first butterfly stage
+  }
   const V *__restrict__ in = reinterpret_cast<const V *>(a.in);
   const V *__restrict__ gx = reinterpret_cast<const V *>(a.gx);
   const V *__restrict__ thi = reinterpret_cast<const V *>(a.tw_hi);
@@ -248,12 +264,15 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
     }
   }
   __syncthreads();
-  cta_fft<V, LOGR, G>(sm, reinterpret_cast<const V *>(a.twR));
+  cta_fft<V, LOGR, G>(sm, twR);
   V *__restrict__ out = reinterpret_cast<V *>(a.out);
   T *__restrict__ smp = reinterpret_cast<T *>(a.samples);
   const bool g_fast_out = logNs >= 0 && (1 << logNs) >= G;
-  // every warp runs the same trip count and its 32 lanes always hold elements
-  // of one batch row (R >= 128 > 32)
+  // All G sub-transforms of the CTA lie in one batch row when S >= G; then each
+  // thread keeps its own maximum and the CTA reduces once.  Otherwise every
+  // warp's lanes hold one row per iteration (R >= 128 > 32).
+  const bool one_row = (1LL << logS) >= G;
+  T tmax = 0;
 #pragma unroll 4
   for (int q = 0; q < ITER; q++) {
     const int lt = threadIdx.x + q * NT;
@@ -274,12 +293,17 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
       }
     }
     if (smp && a.row_max) {
-      const long long bb = __shfl_sync(0xffffffffu, b, 0);
-      const bool uniform = __all_sync(0xffffffffu, b == bb && live);
-      if (uniform) row_max_update(a.row_max, bb, sv);
-      else if (live) atomicMax(reinterpret_cast<typename KeyOf<T>::K *>(a.row_max) + b, key_bits(sv));
+      if (one_row) {
+        tmax = sv > tmax ? sv : tmax;
+      } else {
+        const long long bb = __shfl_sync(0xffffffffu, b, 0);
+        const bool uniform = __all_sync(0xffffffffu, b == bb && live);
+        if (uniform) row_max_update(a.row_max, bb, sv);
+        else if (live) atomicMax(reinterpret_cast<typename KeyOf<T>::K *>(a.row_max) + b, key_bits(sv));
+      }
     }
   }
+  if (smp && a.row_max && one_row && u0 < a.total) row_max_update(a.row_max, u0 >> logS, tmax);
 }
 
 // exp(-2 pi i m / Np) for m in [0, count) at spacing `mul`

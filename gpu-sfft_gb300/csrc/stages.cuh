@@ -22,7 +22,8 @@ struct RunCtl {
   int n_topk;
   int fmax[MAX_LOOPS]; // largest permuted residue per location loop
   unsigned ticket;
-  int pad[3];
+  int err;  // a bounded device-side wait gave up (streaming perm+filter)
+  int pad[2];
 };
 
 struct DevNode {  // == Node (utils.h:42-45)
@@ -40,7 +41,7 @@ int launch_perm_filter(int precision, const void *x, int n, const void *filt, in
 bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops);
 int launch_perm_filter_stream(int precision, const void *x, int n, const void *filt, int w, int B,
                               int loops, const Draws &d, void *bins, int nrlfc, void *y, int W,
-                              cudaStream_t st);
+                              int *err, cudaStream_t st);
 
 // J2 = sorted distinct union of the RLFC blocks, through a W-bit bitmap.
 int launch_j2_merge(const int *J2_blocks, int total, int W, unsigned *bitmap, int *J2,
