@@ -118,7 +118,11 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
                     ((flags & GSFFT_FLAG_FORCE_STREAM) ||
                      (precision == GSFFT_MIXED && stream_bytes < gather_bytes));
   }
-  if (P->use_stream) A(ybuf, V * (size_t)p.RLFC_loops * p.W_RLFC);
+  if (P->use_stream) {
+    P->groups = stream_pf_groups(p.n, p.B, precision);
+    A(ybuf, V * (size_t)p.RLFC_loops * p.W_RLFC);
+    A(bpart, V * (size_t)P->groups * p.loops * p.B);
+  }
 #undef A
   P->floor_rel = (flags & GSFFT_FLAG_RAW_SELECTION) ? 0.0 : 1e-10;
   if (s == GSFFT_OK) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
@@ -148,7 +152,7 @@ void plan_destroy(Plan *P) {
   if (!P) return;
   void *ptrs[] = {P->filt, P->hinv, P->rsamp, P->J2b, P->J2, P->bins, P->bsamp, P->J,
                   P->bm_j2, P->bm_sig, P->tile_tmp, P->vote, P->cand, P->cnt, P->blk,
-                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax, P->ybuf};
+                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax, P->ybuf, P->bpart};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
@@ -232,7 +236,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   BEGIN(ST_PERM_FILTER);
   if (P->use_stream)
     GS_CHECK(launch_perm_filter_stream(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d,
-                                       P->bins, p.RLFC_loops, P->ybuf, p.W_RLFC, &P->ctl->err, st));
+                                       P->bpart, p.RLFC_loops, P->ybuf, p.W_RLFC, &P->ctl->err, st));
   else
     GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d, quirk,
                                 P->bins, st));
@@ -273,7 +277,13 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
     FftIo io;
     io.samples = P->bsamp;
     io.row_max = rmax_b;
-    GS_CHECK(fft_exec(P->fftB, P->bins, P->bins, p.loops, -1, io, st));
+    const void *src = P->bins;
+    if (P->use_stream) {  // the row-group partials are added by the first pass
+      src = P->bpart;
+      io.sum_rows = P->groups;
+      io.sum_stride = (long long)p.loops * p.B;
+    }
+    GS_CHECK(fft_exec(P->fftB, src, P->bins, p.loops, -1, io, st));
   }
   END(ST_BUCKET_FFT);
   BEGIN(ST_CUTOFF);

@@ -173,6 +173,8 @@ struct PassArgs {
   long long gstride;
   void *samples;      // last pass only, or null
   void *row_max;      // per batch row, with samples
+  int nsum;           // first pass: add nsum partial inputs sstride apart
+  long long sstride;
   int write_complex;
 };
 
@@ -242,9 +244,15 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
       const long long b = u >> logS, j = u & Smask;
       const long long m = j + ((long long)r << logS);
       V v;
-      if (u >= a.total) v = mk((T)0, (T)0);
-      else if (gx) v = gx[a.goffs[b] + m * a.gstride];
-      else v = in[b * a.bstride + m];
+      if (u >= a.total) {
+        v = mk((T)0, (T)0);
+      } else if (gx) {
+        v = gx[a.goffs[b] + m * a.gstride];
+      } else {
+        const long long idx = b * a.bstride + m;
+        v = in[idx];
+        for (int s = 1; s < a.nsum; s++) v = cadd(v, in[idx + s * a.sstride]);
+      }
       vbuf[q] = v;
     }
 #pragma unroll
@@ -472,6 +480,8 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
     a.gstride = io.gather_stride;
     a.samples = last ? io.samples : nullptr;
     a.row_max = last ? io.row_max : nullptr;
+    a.nsum = (i == 0) ? io.sum_rows : 1;
+    a.sstride = io.sum_stride;
     a.write_complex = last ? (io.write_complex ? 1 : 0) : 1;
     const long long total_sub = (p.n >> p.logR[i]) * batch;
     a.total = total_sub;

@@ -88,6 +88,10 @@ struct FftIo {
   const void *gather_x = nullptr;
   long long gather_offsets[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // one per batch entry (batch <= 8)
   long long gather_stride = 0;
+  // first-pass loader alternative: element = sum over s < sum_rows of
+  // in[s * sum_stride + index], added in s order (row-group partials)
+  int sum_rows = 1;
+  long long sum_stride = 0;
   // epilogue: |X|^2 (same precision) written to samples[b * n + k]
   void *samples = nullptr;
   // optional: per-row maximum of the samples (bit pattern, u64 for double /

@@ -87,7 +87,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 template <typename T, int L>
 __global__ void __launch_bounds__(ST)
 pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V *__restrict__ filt,
-              int logn, int logB, int w, int rt, int tiles, Draws d, HitTab ht,
+              int logn, int logB, int w, int rt, int tiles, int rows_per_group, Draws d, HitTab ht,
               typename Cx<T>::V *__restrict__ bins, int nrlfc, int logsig,
               typename Cx<T>::V *__restrict__ y, int W, int *err) {
   typedef typename Cx<T>::V V;
@@ -104,7 +104,9 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   const int c0 = blockIdx.x * ST;
   const unsigned c = (unsigned)(c0 + tid);
   const unsigned stage_bytes = (unsigned)(rt * ST * sizeof(V));
-  const int ntile = nb / rt;
+  // row group blockIdx.y covers rows [rbeg, rbeg + rows_per_group)
+  const int rbeg = blockIdx.y * rows_per_group;
+  const int ntile = rows_per_group / rt;
   const int xmul = (int)(sizeof(V) / 8);  // tensor elements are 8-byte words
   V *tile0 = reinterpret_cast<V *>(dsm);
 
@@ -117,8 +119,8 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   __syncthreads();
   if (tid == 0)
     for (int t = 0; t < NSTAGE && t < ntile; t++)
-      tma_load_tile(reinterpret_cast<char *>(tile0) + (size_t)t * stage_bytes, &tmap, c0 * xmul, t * rt,
-                    &bar[t], stage_bytes);
+      tma_load_tile(reinterpret_cast<char *>(tile0) + (size_t)t * stage_bytes, &tmap, c0 * xmul,
+                    rbeg + t * rt, &bar[t], stage_bytes);
 
   // per-loop walk state of this column
   const int residue = w & (B - 1);
@@ -146,9 +148,31 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     re[l] = 0;
     im[l] = 0;
   }
-  unsigned nextmin = NONE;
+  // Advance one loop's walk past the hit at row nm[l] or er[l] (whichever is
+  // smaller) and return its tap index j.
+  auto step = [&](int l) -> int {
+    int j;
+    if (er[l] < nm[l]) {
+      j = tiles;
+      er[l] = NONE;
+    } else {
+      int m = mw[l] + kk[l];
+      if (m >= tiles) m -= tiles;
+      j = (int)(S[l][m] & 255u);
+      kk[l]++;
+      if (kk[l] < tiles) {
+        const int m2 = m + 1 == tiles ? 0 : m + 1;
+        nm[l] = (S[l][m2] >> 8) + sl[l] - (m2 >= mw[l] ? (unsigned)nb : 0u);
+      } else {
+        nm[l] = NONE;
+      }
+    }
+    return j;
+  };
+  // skip the hits of earlier row groups
 #pragma unroll
-  for (int l = 0; l < L; l++) nextmin = min(nextmin, min(nm[l], er[l]));
+  for (int l = 0; l < L; l++)
+    while (min(nm[l], er[l]) < (unsigned)rbeg) (void)step(l);
 
   const unsigned smask = (1u << logsig) - 1u;
   for (int t = 0; t < ntile; t++) {
@@ -157,42 +181,22 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     if (tid == 0 && !mbar_wait(&bar[st], (unsigned)(t / NSTAGE) & 1u)) abort_flag = 1;
     __syncthreads();
     if (abort_flag) break;
-    const unsigned r0 = (unsigned)(t * rt), r1 = r0 + (unsigned)rt;
-    // this column's hits in rows [r0, r1), ascending
-    while (nextmin < r1) {
-      const unsigned r = nextmin;
-      const V xv = tl[(r - r0) * ST + tid];
-      bool done = false;
+    const unsigned r0 = (unsigned)(rbeg + t * rt), r1 = r0 + (unsigned)rt;
+    // loop-major: each lane walks loop l's hits of its column inside the tile,
+    // in ascending row order
 #pragma unroll
-      for (int l = 0; l < L; l++) {
-        if (!done && min(nm[l], er[l]) == r) {
-          done = true;
-          int j;
-          if (er[l] == r) {
-            j = tiles;
-            er[l] = NONE;
-          } else {
-            int m = mw[l] + kk[l];
-            if (m >= tiles) m -= tiles;
-            j = (int)(S[l][m] & 255u);
-            kk[l]++;
-            if (kk[l] < tiles) {
-              int m2 = m + 1 == tiles ? 0 : m + 1;
-              nm[l] = (S[l][m2] >> 8) + sl[l] - (m2 >= mw[l] ? (unsigned)nb : 0u);
-            } else {
-              nm[l] = NONE;
-            }
-          }
-          const V f = __ldg(&filt[((size_t)j << logB) + bl[l]]);
-          re[l] = fma(xv.x, f.x, re[l]);
-          re[l] = fma(-xv.y, f.y, re[l]);
-          im[l] = fma(xv.x, f.y, im[l]);
-          im[l] = fma(xv.y, f.x, im[l]);
-        }
+    for (int l = 0; l < L; l++) {
+      while (true) {
+        const unsigned r = min(nm[l], er[l]);
+        if (r >= r1) break;
+        const V xv = tl[(r - r0) * ST + tid];
+        const int j = step(l);
+        const V f = __ldg(&filt[((size_t)j << logB) + bl[l]]);
+        re[l] = fma(xv.x, f.x, re[l]);
+        re[l] = fma(-xv.y, f.y, re[l]);
+        im[l] = fma(xv.x, f.y, im[l]);
+        im[l] = fma(xv.y, f.x, im[l]);
       }
-      nextmin = NONE;
-#pragma unroll
-      for (int l = 0; l < L; l++) nextmin = min(nextmin, min(nm[l], er[l]));
     }
     // RLFC sub-samples held by this tile: columns c == off (mod n/W)
     for (int rr = 0; rr < nrlfc; rr++) {
@@ -211,7 +215,7 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     if (tid == 0 && t + NSTAGE < ntile) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tma_load_tile(reinterpret_cast<char *>(tile0) + (size_t)st * stage_bytes, &tmap, c0 * xmul,
-                    (t + NSTAGE) * rt, &bar[st], stage_bytes);
+                    rbeg + (t + NSTAGE) * rt, &bar[st], stage_bytes);
     }
   }
   if (abort_flag) {
@@ -222,8 +226,19 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     }
     return;
   }
+  // partial sums of this row group: bins[group][l][b]
+  V *part = bins + (size_t)blockIdx.y * L * B;
 #pragma unroll
-  for (int l = 0; l < L; l++) bins[(size_t)l * B + bl[l]] = mk(re[l], im[l]);
+  for (int l = 0; l < L; l++) part[(size_t)l * B + bl[l]] = mk(re[l], im[l]);
+}
+
+template <typename V>
+__global__ void sum_partials_kernel(const V *__restrict__ part, int groups, long long count, V *out) {
+  const long long i = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (i >= count) return;
+  V v = part[i];
+  for (int g = 1; g < groups; g++) v = cadd(v, part[(long long)g * count + i]);
+  out[i] = v;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -253,8 +268,8 @@ unsigned inv_odd(unsigned a) {  // a^-1 mod 2^32 for odd a (Newton)
 
 template <typename T, int L>
 int launch_L(const CUtensorMap &tm, const void *filt, int logn, int logB, int w, int rt, int tiles,
-             const Draws &d, const HitTab &ht, void *bins, int nrlfc, int logsig, void *y, int W,
-             int *err, cudaStream_t st) {
+             int groups, const Draws &d, const HitTab &ht, void *bins, int nrlfc, int logsig, void *y,
+             int W, int *err, cudaStream_t st) {
   typedef typename Cx<T>::V V;
   const int B = 1 << logB;
   const int smem = NSTAGE * rt * ST * (int)sizeof(V);
@@ -264,18 +279,20 @@ int launch_L(const CUtensorMap &tm, const void *filt, int logn, int logB, int w,
                                  smem));
     attr = true;
   }
-  pf_tma_kernel<T, L><<<B / ST, ST, smem, st>>>(tm, (const V *)filt, logn, logB, w, rt, tiles, d, ht,
-                                               (V *)bins, nrlfc, logsig, (V *)y, W, err);
+  const int rows_per_group = (1 << (logn - logB)) / groups;
+  pf_tma_kernel<T, L><<<dim3(B / ST, groups), ST, smem, st>>>(tm, (const V *)filt, logn, logB, w, rt,
+                                                              tiles, rows_per_group, d, ht, (V *)bins,
+                                                              nrlfc, logsig, (V *)y, W, err);
   return GSFFT_OK;
 }
 
 template <typename T>
 int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int logB, int w, int rt,
-             int tiles, const Draws &d, const HitTab &ht, void *bins, int nrlfc, int logsig, void *y,
-             int W, int *err, cudaStream_t st) {
+             int tiles, int groups, const Draws &d, const HitTab &ht, void *bins, int nrlfc,
+             int logsig, void *y, int W, int *err, cudaStream_t st) {
   switch (loops) {
 #define C(LL) \
-  case LL: return launch_L<T, LL>(tm, filt, logn, logB, w, rt, tiles, d, ht, bins, nrlfc, logsig, y, W, err, st);
+  case LL: return launch_L<T, LL>(tm, filt, logn, logB, w, rt, tiles, groups, d, ht, bins, nrlfc, logsig, y, W, err, st);
     C(2) C(3) C(4) C(5) C(6) C(7) C(8) C(9) C(10) C(11) C(12) C(13) C(14) C(15) C(16)
 #undef C
     default: return GSFFT_ERR_UNSUPPORTED;
@@ -284,11 +301,33 @@ int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int l
 
 }  // namespace
 
+int launch_sum_partials(int precision, const void *part, int groups, long long count, void *out,
+                        cudaStream_t st) {
+  const unsigned grid = (unsigned)((count + 255) / 256);
+  if (precision == GSFFT_FP64)
+    sum_partials_kernel<double2><<<grid, 256, 0, st>>>((const double2 *)part, groups, count,
+                                                       (double2 *)out);
+  else
+    sum_partials_kernel<float2><<<grid, 256, 0, st>>>((const float2 *)part, groups, count,
+                                                      (float2 *)out);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
 bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops) {
   if (loops < 2 || loops > MAXL || B < ST || (B % ST) != 0 || n / B < 2) return false;
   if (RLFC_loops > MAX_RLFC_LOOPS || (W > 0 && n / W > B)) return false;
   if (n / B > (1 << 23)) return false;  // row offsets must fit 24 bits
   return encode_fn() != nullptr;
+}
+
+int stream_pf_groups(int n, int B, int precision) {
+  const int nb = n / B;
+  const int rt = std::min(nb, precision == GSFFT_FP64 ? 16 : 32);
+  // about 1200 CTAs (two or more waves of the 152 SMs), each group >= one tile
+  int groups = 1;
+  while ((long long)(B / ST) * groups * 2 <= 1216 && nb / (groups * 2) >= rt) groups *= 2;
+  return groups;
 }
 
 int launch_perm_filter_stream(int precision, const void *x, int n, const void *filt, int w, int B,
@@ -316,7 +355,8 @@ int launch_perm_filter_stream(int precision, const void *x, int n, const void *f
   // x as a 2-D tensor of 8-byte words: nb rows of B (FP32) or 2B (FP64) words
   const bool dbl = precision == GSFFT_FP64;
   const int es = dbl ? 16 : 8;
-  int rt = std::min(nb, dbl ? 16 : 32);
+  const int rt = std::min(nb, dbl ? 16 : 32);
+  const int groups = stream_pf_groups(n, B, precision);
   CUtensorMap tm;
   const cuuint64_t gdim[2] = {(cuuint64_t)B * (es / 8), (cuuint64_t)nb};
   const cuuint64_t gstride[1] = {(cuuint64_t)B * es};
@@ -330,10 +370,10 @@ int launch_perm_filter_stream(int precision, const void *x, int n, const void *f
     set_last_error("cuTensorMapEncodeTiled failed (%d)", (int)cr);
     return GSFFT_ERR_CUDA;
   }
-  int s = dbl ? dispatch<double>(loops, tm, filt, logn, logB, w, rt, tiles, d, ht, bins, nrlfc, logsig,
-                                 y, W, err, st)
-              : dispatch<float>(loops, tm, filt, logn, logB, w, rt, tiles, d, ht, bins, nrlfc, logsig,
-                                y, W, err, st);
+  int s = dbl ? dispatch<double>(loops, tm, filt, logn, logB, w, rt, tiles, groups, d, ht, bins,
+                                 nrlfc, logsig, y, W, err, st)
+              : dispatch<float>(loops, tm, filt, logn, logB, w, rt, tiles, groups, d, ht, bins, nrlfc,
+                                logsig, y, W, err, st);
   if (s != GSFFT_OK) return s;
   GS_LAUNCHED();
   return GSFFT_OK;
