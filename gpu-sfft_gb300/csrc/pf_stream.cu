@@ -38,7 +38,7 @@ namespace gsfft {
 namespace {
 
 constexpr int ST = 128;      // columns per CTA
-constexpr int NSTAGE = 3;    // tiles in flight
+constexpr int NSTAGE = 2;    // tiles in flight
 constexpr int MAXT = 32;     // full tiles of taps per bucket (w / B) supported
 constexpr int MAXL = 16;     // loops supported
 constexpr unsigned NONE = 0x7fffffffu;
@@ -169,10 +169,31 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     }
     return j;
   };
-  // skip the hits of earlier row groups
+  // skip the hits of earlier row groups: the rotated rows are ascending, so
+  // the first rotated position with row >= rbeg is found by binary search
+  if (rbeg > 0) {
 #pragma unroll
-  for (int l = 0; l < L; l++)
-    while (min(nm[l], er[l]) < (unsigned)rbeg) (void)step(l);
+    for (int l = 0; l < L; l++) {
+      int lo = 0, hi = tiles;  // first k in [0, tiles) with row(k) >= rbeg
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        int m = mw[l] + mid;
+        if (m >= tiles) m -= tiles;
+        const unsigned row = (S[l][m] >> 8) + sl[l] - (m >= mw[l] ? (unsigned)nb : 0u);
+        if (row < (unsigned)rbeg) lo = mid + 1;
+        else hi = mid;
+      }
+      kk[l] = lo;
+      if (lo < tiles) {
+        int m = mw[l] + lo;
+        if (m >= tiles) m -= tiles;
+        nm[l] = (S[l][m] >> 8) + sl[l] - (m >= mw[l] ? (unsigned)nb : 0u);
+      } else {
+        nm[l] = NONE;
+      }
+      if (er[l] < (unsigned)rbeg) er[l] = NONE;
+    }
+  }
 
   const unsigned smask = (1u << logsig) - 1u;
   for (int t = 0; t < ntile; t++) {
@@ -198,14 +219,15 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
         im[l] = fma(xv.y, f.x, im[l]);
       }
     }
-    // RLFC sub-samples held by this tile: columns c == off (mod n/W)
+    // RLFC sub-samples held by this tile: columns c == off (mod n/W); with
+    // n/W <= 128 there are 128 >> logsig of them, else at most one
     for (int rr = 0; rr < nrlfc; rr++) {
       const unsigned off = (unsigned)d.offs[rr];
       const unsigned first = ((off - (unsigned)c0) & smask);  // first matching column index
       if (first >= (unsigned)ST) continue;
-      const int ncol = (int)((ST - 1 - first) >> logsig) + 1;
-      for (int e = tid; e < rt * ncol; e += ST) {
-        const int row = e / ncol, ci = e % ncol;
+      const int lognc = logsig >= 7 ? 0 : 7 - logsig;         // log2 of the column count
+      for (int e = tid; e < (rt << lognc); e += ST) {
+        const int row = e >> lognc, ci = e & ((1 << lognc) - 1);
         const unsigned cc = first + ((unsigned)ci << logsig);
         const unsigned tpos = ((r0 + row) << logB) + (unsigned)c0 + cc;
         y[(size_t)rr * W + ((tpos - off) >> logsig)] = tl[row * ST + cc];
@@ -323,10 +345,11 @@ bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops) {
 
 int stream_pf_groups(int n, int B, int precision) {
   const int nb = n / B;
-  const int rt = std::min(nb, precision == GSFFT_FP64 ? 16 : 32);
-  // about 1200 CTAs (two or more waves of the 152 SMs), each group >= one tile
+  const int rt = std::min(nb, precision == GSFFT_FP64 ? 8 : 16);
+  // at least ~2400 CTAs (several waves of ~5 resident CTAs on 152 SMs), each
+  // group at least one tile
   int groups = 1;
-  while ((long long)(B / ST) * groups * 2 <= 1216 && nb / (groups * 2) >= rt) groups *= 2;
+  while ((long long)(B / ST) * groups < 2400 && nb / (groups * 2) >= rt) groups *= 2;
   return groups;
 }
 
@@ -355,7 +378,7 @@ int launch_perm_filter_stream(int precision, const void *x, int n, const void *f
   // x as a 2-D tensor of 8-byte words: nb rows of B (FP32) or 2B (FP64) words
   const bool dbl = precision == GSFFT_FP64;
   const int es = dbl ? 16 : 8;
-  const int rt = std::min(nb, dbl ? 16 : 32);
+  const int rt = std::min(nb, dbl ? 8 : 16);
   const int groups = stream_pf_groups(n, B, precision);
   CUtensorMap tm;
   const cuuint64_t gdim[2] = {(cuuint64_t)B * (es / 8), (cuuint64_t)nb};
