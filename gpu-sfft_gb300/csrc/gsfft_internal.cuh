@@ -116,9 +116,11 @@ int fft_launches(const FftPlan &p);
 struct SelectScratch {
   void *hist = nullptr;        // batch * 2048 uint32
   void *state = nullptr;       // batch * SelState
-  void *tiles = nullptr;       // batch * max_tiles * 2 uint32
+  void *tiles = nullptr;       // batch * max_tiles * 4 uint32
+  void *coop_hist = nullptr;   // single-launch form: 6 passes x 8 rows x 2048 bins
   int max_batch = 0, max_tiles = 0;
 };
+extern bool g_select_coop;  // use the single-launch cooperative select
 int select_scratch_init(SelectScratch &s, int max_batch, long long max_size);
 void select_scratch_free(SelectScratch &s);
 // row_max (optional, per row, bit pattern of the largest sample) with

@@ -349,7 +349,7 @@ int stream_pf_groups(int n, int B, int precision) {
   // at least ~2400 CTAs (several waves of ~5 resident CTAs on 152 SMs), each
   // group at least one tile
   int groups = 1;
-  while ((long long)(B / ST) * groups < 2400 && nb / (groups * 2) >= rt) groups *= 2;
+  while ((long long)(B / ST) * groups < 1500 && nb / (groups * 2) >= rt) groups *= 2;
   return groups;
 }
 

@@ -24,6 +24,8 @@
 // same ids.
 #include "gsfft_internal.cuh"
 
+#include <cooperative_groups.h>
+
 namespace gsfft {
 
 namespace {
@@ -343,6 +345,275 @@ int select_impl(const void *keys, long long size, const int *size_dev, int num, 
   return GSFFT_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Single-launch form: the same passes in one cooperative kernel separated by
+// grid-wide syncs.  Every CTA re-derives the digit of each row from the shared
+// histogram, so one sync per pass suffices.  Histograms are left zeroed for
+// the next call.
+// ---------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+
+constexpr int MAXB = 8;  // rows per cooperative call
+
+struct CoopArgs {
+  const void *keys;
+  long long size;        // capacity per row
+  const int *size_dev;   // live size (batch 1) or null
+  int num, batch;
+  long long row_stride;
+  int *out;
+  long long out_stride;
+  int *count_out;
+  const void *row_max;
+  double floor_rel;
+  unsigned *hist;        // [6][MAXB][HIST_BINS], zero on entry and on exit
+  unsigned *tiles;       // [MAXB][max_tiles][2]
+  int max_tiles;
+};
+
+struct RowSt {
+  unsigned long long floor, prefix;
+  long long rank;
+  int size, take_all;
+};
+
+template <typename K>
+__global__ void __launch_bounds__(SEL_THREADS) sel_coop_kernel(CoopArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ unsigned sh[HIST_BINS];
+  __shared__ unsigned warp_sums[SEL_THREADS / 32];
+  __shared__ RowSt rs[MAXB];
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int kb = (int)sizeof(K) * 8;
+  const int w64[6] = {11, 11, 11, 11, 10, 10};
+  const int w32[3] = {11, 11, 10};
+  const int npass = kb == 64 ? 6 : 3;
+  if (tid < a.batch) {
+    const int b = tid;
+    long long sz = a.size;
+    if (a.size_dev) {
+      long long dv = *a.size_dev;
+      sz = dv < a.size ? dv : a.size;
+      if (sz < 0) sz = 0;
+    }
+    RowSt r;
+    r.floor = 0;
+    if (a.row_max && a.floor_rel > 0.0) {
+      if (kb == 64) {
+        const double m = __longlong_as_double((long long)reinterpret_cast<const unsigned long long *>(a.row_max)[b]);
+        r.floor = (unsigned long long)__double_as_longlong(m * a.floor_rel);
+      } else {
+        const float m = __uint_as_float(reinterpret_cast<const unsigned *>(a.row_max)[b]);
+        r.floor = __float_as_uint((float)((double)m * a.floor_rel));
+      }
+    }
+    r.prefix = 0;
+    r.size = (int)sz;
+    r.take_all = sz <= a.num ? 1 : 0;
+    r.rank = sz - a.num - 1;
+    rs[b] = r;
+  }
+  __syncthreads();
+  const int T = (int)((a.size + SEL_TILE - 1) / SEL_TILE);
+  const int nitems = a.batch * T;
+  int shift = kb;
+  for (int p = 0; p < npass; p++) {
+    const int width = kb == 64 ? w64[p] : w32[p];
+    shift -= width;
+    const unsigned dmask = (1u << width) - 1u;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+      const int b = it / T, tile = it - b * T;
+      const RowSt r = rs[b];
+      if (r.take_all || (long long)tile * SEL_TILE >= r.size) continue;
+      for (int i = tid; i < HIST_BINS; i += SEL_THREADS) sh[i] = 0;
+      __syncthreads();
+      const unsigned long long hi_mask =
+          (shift + width >= kb) ? 0ull : (~0ull << (shift + width)) & (kb == 64 ? ~0ull : 0xffffffffull);
+      const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
+      const long long base = (long long)tile * SEL_TILE;
+#pragma unroll 4
+      for (int q = 0; q < SEL_ITEMS; q++) {
+        const long long i = base + q * SEL_THREADS + tid;
+        bool hit = false;
+        unsigned digit = 0;
+        if (i < r.size) {
+          const unsigned long long k = (unsigned long long)load_key<K>(row, i, (K)r.floor);
+          hit = (k & hi_mask) == r.prefix;
+          digit = (unsigned)(k >> shift) & dmask;
+        }
+        const unsigned key = hit ? digit : (0x80000000u | (unsigned)lane);
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (hit && lane == __ffs(peers) - 1) atomicAdd(&sh[digit], (unsigned)__popc(peers));
+      }
+      __syncthreads();
+      unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
+      for (int i = tid; i < HIST_BINS; i += SEL_THREADS)
+        if (sh[i]) atomicAdd(&gh[i], sh[i]);
+      __syncthreads();
+    }
+    grid.sync();
+    // every CTA finds the digit of each row holding its remaining rank
+    for (int b = 0; b < a.batch; b++) {
+      if (rs[b].take_all) continue;
+      const unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
+      const int per = HIST_BINS / SEL_THREADS;
+      unsigned local[HIST_BINS / SEL_THREADS];
+      unsigned sum = 0;
+#pragma unroll
+      for (int q = 0; q < per; q++) {
+        local[q] = __ldcg(&gh[tid * per + q]);
+        sum += local[q];
+      }
+      unsigned tot;
+      const unsigned before = block_excl_scan(sum, warp_sums, &tot);
+      const long long rank = rs[b].rank;
+      const unsigned long long prefix = rs[b].prefix;
+      __syncthreads();
+      unsigned run = before;
+#pragma unroll
+      for (int q = 0; q < per; q++) {
+        if ((long long)run <= rank && rank < (long long)run + local[q]) {
+          rs[b].prefix = prefix | ((unsigned long long)(tid * per + q) << shift);
+          rs[b].rank = rank - run;
+        }
+        run += local[q];
+      }
+      __syncthreads();
+    }
+  }
+  // counting pass
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int b = it / T, tile = it - b * T;
+    const RowSt r = rs[b];
+    if (r.take_all) continue;
+    const K thr = (K)r.prefix;
+    const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
+    const long long base = (long long)tile * SEL_TILE;
+    unsigned gt = 0, eq = 0;
+    if (base < r.size) {
+#pragma unroll 4
+      for (int q = 0; q < SEL_ITEMS; q++) {
+        const long long i = base + q * SEL_THREADS + tid;
+        if (i < r.size) {
+          const K k = load_key<K>(row, i, (K)r.floor);
+          gt += k > thr;
+          eq += k == thr;
+        }
+      }
+    }
+    unsigned tgt, teq;
+    block_excl_scan(gt, warp_sums, &tgt);
+    block_excl_scan(eq, warp_sums, &teq);
+    if (tid == 0) {
+      a.tiles[((size_t)b * a.max_tiles + tile) * 2 + 0] = tgt;
+      a.tiles[((size_t)b * a.max_tiles + tile) * 2 + 1] = teq;
+    }
+  }
+  grid.sync();
+  // every CTA has read the histograms: zero them for the next call
+  for (int i = blockIdx.x * SEL_THREADS + tid; i < npass * MAXB * HIST_BINS; i += gridDim.x * SEL_THREADS)
+    a.hist[i] = 0;
+  // writing pass
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int b = it / T, tile = it - b * T;
+    const RowSt r = rs[b];
+    int *o = a.out + (size_t)b * a.out_stride;
+    const long long base = (long long)tile * SEL_TILE;
+    if (r.take_all) {
+      for (int q = 0; q < SEL_ITEMS; q++) {
+        const long long i = base + q * SEL_THREADS + tid;
+        if (i < r.size) o[i] = (int)i;
+      }
+      continue;
+    }
+    if (base >= r.size) continue;
+    // prefix of this tile and totals of the row
+    unsigned bg = 0, be = 0, tg = 0;
+    const unsigned *tb = a.tiles + (size_t)b * a.max_tiles * 2;
+    for (int t2 = tid; t2 < T; t2 += SEL_THREADS) {
+      const unsigned vg = __ldcg(&tb[t2 * 2]), ve = __ldcg(&tb[t2 * 2 + 1]);
+      if (t2 < tile) { bg += vg; be += ve; }
+      tg += vg;
+    }
+    unsigned s_bg, s_be, s_tg;
+    block_excl_scan(bg, warp_sums, &s_bg);
+    block_excl_scan(be, warp_sums, &s_be);
+    block_excl_scan(tg, warp_sums, &s_tg);
+    const unsigned need_eq = (unsigned)(a.num - (int)s_tg);
+    unsigned gt_run = s_bg, eq_run = s_be;
+    const K thr = (K)r.prefix;
+    const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
+    for (int q = 0; q < SEL_ITEMS; q++) {
+      const long long i = base + q * SEL_THREADS + tid;
+      unsigned g = 0, e = 0;
+      if (i < r.size) {
+        const K k = load_key<K>(row, i, (K)r.floor);
+        g = k > thr;
+        e = k == thr;
+      }
+      unsigned cg_, ce;
+      const unsigned pg = block_excl_scan(g, warp_sums, &cg_);
+      const unsigned pe = block_excl_scan(e, warp_sums, &ce);
+      const unsigned eq_before = eq_run + pe;
+      if (g || (e && eq_before < need_eq)) {
+        const unsigned pos = gt_run + pg + (eq_before < need_eq ? eq_before : need_eq);
+        if (pos < (unsigned)a.num) o[pos] = (int)i;
+      }
+      gt_run += cg_;
+      eq_run += ce;
+    }
+  }
+  if (a.count_out && blockIdx.x == 0 && tid < a.batch)
+    a.count_out[tid] = rs[tid].take_all ? rs[tid].size : a.num;
+}
+
+template <typename K>
+int coop_grid() {
+  static int g = 0;
+  if (!g) {
+    int dev = 0, sms = 0, per = 0, coop = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (!coop) return -1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K>, SEL_THREADS, 0);
+    g = per > 0 ? per * sms : -1;
+  }
+  return g;
+}
+
+template <typename K>
+int select_coop_impl(const void *keys, long long size, const int *size_dev, int num, int batch,
+                     long long row_stride, int *out, long long out_stride, int *count_out,
+                     SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
+  const long long tiles = (size + SEL_TILE - 1) / SEL_TILE;
+  const int maxg = coop_grid<K>();
+  if (maxg <= 0) return GSFFT_ERR_UNSUPPORTED;
+  CoopArgs a;
+  a.keys = keys;
+  a.size = size;
+  a.size_dev = size_dev;
+  a.num = num;
+  a.batch = batch;
+  a.row_stride = row_stride;
+  a.out = out;
+  a.out_stride = out_stride;
+  a.count_out = count_out;
+  a.row_max = row_max;
+  a.floor_rel = floor_rel;
+  a.hist = reinterpret_cast<unsigned *>(s.coop_hist);
+  a.tiles = reinterpret_cast<unsigned *>(s.tiles);
+  a.max_tiles = s.max_tiles;
+  const long long items = tiles * batch;
+  const int grid = (int)(items < maxg ? items : maxg);
+  void *args[] = {&a};
+  GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K>, dim3(grid), dim3(SEL_THREADS),
+                                      args, 0, st));
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
 }  // namespace
 
 int select_scratch_init(SelectScratch &s, int max_batch, long long max_size) {
@@ -353,6 +624,8 @@ int select_scratch_init(SelectScratch &s, int max_batch, long long max_size) {
   GS_CUDA(cudaMalloc(&s.state, sizeof(SelState) * max_batch));
   GS_CUDA(cudaMalloc(&s.tiles, sizeof(unsigned) * 4 * (size_t)s.max_tiles * max_batch));
   GS_CUDA(cudaMemset(s.state, 0, sizeof(SelState) * max_batch));
+  GS_CUDA(cudaMalloc(&s.coop_hist, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
+  GS_CUDA(cudaMemset(s.coop_hist, 0, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
   return GSFFT_OK;
 }
 
@@ -360,15 +633,27 @@ void select_scratch_free(SelectScratch &s) {
   if (s.hist) cudaFree(s.hist);
   if (s.state) cudaFree(s.state);
   if (s.tiles) cudaFree(s.tiles);
-  s.hist = s.state = s.tiles = nullptr;
+  if (s.coop_hist) cudaFree(s.coop_hist);
+  s.hist = s.state = s.tiles = s.coop_hist = nullptr;
 }
 
 int select_launches(int key_bytes) { return key_bytes == 8 ? 9 : 6; }
+
+bool g_select_coop = true;  // single-launch select when the device supports it
 
 int select_top(const void *keys, int key_bytes, long long size, const int *size_dev, int num,
                int batch, long long row_stride, int *out, long long out_stride, int *count_out,
                SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
   if (size_dev && batch != 1) return GSFFT_ERR_PARAM;
+  if (g_select_coop && batch <= MAXB && batch <= s.max_batch &&
+      (size + SEL_TILE - 1) / SEL_TILE <= s.max_tiles) {
+    int r = key_bytes == 8
+                ? select_coop_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride, out,
+                                                       out_stride, count_out, s, st, row_max, floor_rel)
+                : select_coop_impl<unsigned int>(keys, size, size_dev, num, batch, row_stride, out,
+                                                 out_stride, count_out, s, st, row_max, floor_rel);
+    if (r != GSFFT_ERR_UNSUPPORTED) return r;
+  }
   if (key_bytes == 8)
     return select_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride, out,
                                            out_stride, count_out, s, st, row_max, floor_rel);
