@@ -228,7 +228,8 @@ def run_ours(args, cfg):
     x32 = x64.to(torch.complex64)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
-    plans = {"fp64": gsfft.Plan(p, gsfft.FP64), "mixed": gsfft.Plan(p, gsfft.MIXED)}
+    pf_flag = {"auto": 0, "gather": gsfft.FLAG_FORCE_GATHER, "stream": gsfft.FLAG_FORCE_STREAM}[args.pf]
+    plans = {"fp64": gsfft.Plan(p, gsfft.FP64, pf_flag), "mixed": gsfft.Plan(p, gsfft.MIXED, pf_flag)}
     for pl in plans.values():
         pl.set_filter(d_ft.data_ptr(), d_ff.data_ptr(), sh)
     xin = {"fp64": x64, "mixed": x32}
@@ -273,7 +274,7 @@ def run_ours(args, cfg):
     ms32, st32, clocks = timed("mixed", sampler)
     if args.only_mixed:
         if rank == 0:
-            print(json.dumps({"profile_run": True, "ms_per_step": ms32 / args.steps,
+            print(json.dumps({"profile_run": True, "pf": args.pf, "ms_per_step": ms32 / args.steps,
                               "stage_ms": st32, "launches_per_run": plans["mixed"].launches_per_run()}))
         return 0
 
@@ -402,6 +403,8 @@ def main():
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="headline", choices=["headline", "small"],
                     help="small: n=2^25, k=4000 (same W_RLFC) for profiler captures")
+    ap.add_argument("--pf", default="auto", choices=["auto", "gather", "stream"],
+                    help="perm+filter form (auto: by the plan's DRAM byte model)")
     ap.add_argument("--only-mixed", action="store_true",
                     help="time only the mixed path and print its stage times (profiling runs)")
     args = ap.parse_args()

@@ -231,44 +231,84 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
   const long long u0 = (long long)blockIdx.x * G;
   const int hmask = (1 << a.tw_h) - 1;
   const bool g_fast_in = logS >= 0 && (1LL << logS) >= G;
-  constexpr int LB = ITER < 4 ? ITER : 4;  // loads in flight per thread
+  if (a.nsum <= 1) {
+    // every element straight into shared memory with cp.async: all ITER loads
+    // of a thread in flight, no registers held
 #pragma unroll
-  for (int q0 = 0; q0 < ITER; q0 += LB) {
-    V vbuf[LB];
-#pragma unroll
-    for (int q = 0; q < LB; q++) {
-      const int lt = threadIdx.x + (q0 + q) * NT;
+    for (int q = 0; q < ITER; q++) {
+      const int lt = threadIdx.x + q * NT;
       int g, r;
       if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
       const long long u = u0 + g;
       const long long b = u >> logS, j = u & Smask;
       const long long m = j + ((long long)r << logS);
-      V v;
+      V *dst = &sm[g * RP + padded(r)];
       if (u >= a.total) {
-        v = mk((T)0, (T)0);
-      } else if (gx) {
-        v = gx[a.goffs[b] + m * a.gstride];
+        *dst = mk((T)0, (T)0);
       } else {
-        const long long idx = b * a.bstride + m;
-        v = in[idx];
-        for (int s = 1; s < a.nsum; s++) v = cadd(v, in[idx + s * a.sstride]);
+        const V *src = gx ? &gx[a.goffs[b] + m * a.gstride] : &in[b * a.bstride + m];
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                     "l"(src), "n"(sizeof(V))
+                     : "memory");
       }
-      vbuf[q] = v;
     }
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+    if (a.inverse || logNs > 0) {
+      // each thread rewrites only the elements it loaded: no barrier needed here
 #pragma unroll
-    for (int q = 0; q < LB; q++) {
-      const int lt = threadIdx.x + (q0 + q) * NT;
-      int g, r;
-      if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
-      V v = vbuf[q];
-      if (a.inverse) v.y = -v.y;
-      if (logNs > 0) {
-        const long long j = (u0 + g) & Smask;
-        const long long mm = (j & Nsmask) * r;  // < Ns * R
-        V w = cmul(thi[mm >> a.tw_h], tlo[mm & hmask]);
-        v = cmul(v, w);
+      for (int q = 0; q < ITER; q++) {
+        const int lt = threadIdx.x + q * NT;
+        int g, r;
+        if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+        V *p = &sm[g * RP + padded(r)];
+        V v = *p;
+        if (a.inverse) v.y = -v.y;
+        if (logNs > 0) {
+          const long long j = (u0 + g) & Smask;
+          const long long mm = (j & Nsmask) * r;  // < Ns * R
+          V w = cmul(thi[mm >> a.tw_h], tlo[mm & hmask]);
+          v = cmul(v, w);
+        }
+        *p = v;
       }
-      sm[g * RP + padded(r)] = v;
+    }
+  } else {
+    // row-group partials added on load (first pass after the streaming perm+filter)
+    constexpr int LB = ITER < 4 ? ITER : 4;
+#pragma unroll
+    for (int q0 = 0; q0 < ITER; q0 += LB) {
+      V vbuf[LB];
+#pragma unroll
+      for (int q = 0; q < LB; q++) {
+        const int lt = threadIdx.x + (q0 + q) * NT;
+        int g, r;
+        if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+        const long long u = u0 + g;
+        const long long b = u >> logS, j = u & Smask;
+        const long long m = j + ((long long)r << logS);
+        V v = mk((T)0, (T)0);
+        if (u < a.total) {
+          const long long idx = b * a.bstride + m;
+          v = in[idx];
+          for (int s2 = 1; s2 < a.nsum; s2++) v = cadd(v, in[idx + s2 * a.sstride]);
+        }
+        vbuf[q] = v;
+      }
+#pragma unroll
+      for (int q = 0; q < LB; q++) {
+        const int lt = threadIdx.x + (q0 + q) * NT;
+        int g, r;
+        if (g_fast_in) { g = lt % G; r = lt / G; } else { r = lt % R; g = lt / R; }
+        V v = vbuf[q];
+        if (a.inverse) v.y = -v.y;
+        if (logNs > 0) {
+          const long long j = (u0 + g) & Smask;
+          const long long mm = (j & Nsmask) * r;
+          V w = cmul(thi[mm >> a.tw_h], tlo[mm & hmask]);
+          v = cmul(v, w);
+        }
+        sm[g * RP + padded(r)] = v;
+      }
     }
   }
   __syncthreads();
