@@ -127,8 +127,31 @@ __device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR, int
     if (Ns > 1) {
       const int k = t % Ns;
       const int step = R / (Ns * E);
+      if (sizeof(v[0][0].x) == 8 || E < 4) {
+        // FP64: exact table entries (its FP64 pipe, not shared memory, is the limit)
 #pragma unroll
-      for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], twR[k * e * step]);
+        for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], twR[k * e * step]);
+      } else {
+        // FP32: two table reads (w, w^4), other powers by products at most four
+        // deep -- the strided table reads were the shared-memory bank hot spot
+        V w[E];
+        w[1] = twR[k * step];
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
+        w[4] = twR[4 * k * step];
+#pragma unroll
+        for (int e = 5; e < 8 && e < E; e++) w[e] = cmul(w[4], w[e - 4]);
+        if (E == 16) {
+          w[8] = cmul(w[4], w[4]);
+#pragma unroll
+          for (int e = 9; e < 12; e++) w[e] = cmul(w[8], w[e - 8]);
+          w[12] = cmul(w[8], w[4]);
+#pragma unroll
+          for (int e = 13; e < 16; e++) w[e] = cmul(w[12], w[e - 12]);
+        }
+#pragma unroll
+        for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], w[e]);
+      }
     }
     dft_reg<V, E>(v[q]);
   }

@@ -85,14 +85,15 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 }
 
 template <typename T, int L>
-__global__ void __launch_bounds__(ST)
+__global__ void __launch_bounds__(ST, 5)
 pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V *__restrict__ filt,
               int logn, int logB, int w, int rt, int tiles, int rows_per_group, Draws d, HitTab ht,
               typename Cx<T>::V *__restrict__ bins, int nrlfc, int logsig,
               typename Cx<T>::V *__restrict__ y, int W, int *err) {
   typedef typename Cx<T>::V V;
   extern __shared__ __align__(128) unsigned char dsm[];
-  __shared__ unsigned S[L][MAXT];
+  // each loop's sorted list twice in a row, so a rotated walk needs no wrap
+  __shared__ unsigned S2[L][2 * MAXT];
   __shared__ __align__(8) unsigned long long bar[NSTAGE];
   __shared__ int abort_flag;
   const int tid = threadIdx.x;
@@ -104,13 +105,15 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   const int c0 = blockIdx.x * ST;
   const unsigned c = (unsigned)(c0 + tid);
   const unsigned stage_bytes = (unsigned)(rt * ST * sizeof(V));
-  // row group blockIdx.y covers rows [rbeg, rbeg + rows_per_group)
-  const int rbeg = blockIdx.y * rows_per_group;
+  const int rbeg = blockIdx.y * rows_per_group;  // this CTA's rows: [rbeg, rbeg + rows_per_group)
   const int ntile = rows_per_group / rt;
   const int xmul = (int)(sizeof(V) / 8);  // tensor elements are 8-byte words
   V *tile0 = reinterpret_cast<V *>(dsm);
 
-  for (int e = tid; e < L * MAXT; e += ST) S[e / MAXT][e % MAXT] = ht.s[e / MAXT][e % MAXT];
+  for (int e = tid; e < L * 2 * MAXT; e += ST) {
+    const int l = e / (2 * MAXT), m = e % (2 * MAXT);
+    S2[l][m] = m < tiles ? ht.s[l][m] : (m < 2 * tiles ? ht.s[l][m - tiles] : 0u);
+  }
   if (tid == 0) {
     abort_flag = 0;
     for (int s = 0; s < NSTAGE; s++) mbar_init(&bar[s], 1);
@@ -122,9 +125,11 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
       tma_load_tile(reinterpret_cast<char *>(tile0) + (size_t)t * stage_bytes, &tmap, c0 * xmul,
                     rbeg + t * rt, &bar[t], stage_bytes);
 
-  // per-loop walk state of this column
+  // Walk state per loop.  Rotated position k of the column's hit list is
+  // doubled-list entry m = mw + k; its row is v + s - nb when m < tiles (the
+  // entry wrapped past nb) and v + s otherwise.
   const int residue = w & (B - 1);
-  int bl[L], mw[L], kk[L];
+  int bl[L], mc[L], me[L];
   unsigned sl[L], nm[L], er[L];
   T re[L], im[L];
 #pragma unroll
@@ -134,65 +139,32 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     bl[l] = (int)(prod & (unsigned)(B - 1));
     const unsigned q = (prod & nmask) >> logB;
     sl[l] = (0u - q * ht.beta[l]) & nbm;
-    int m = 0;  // first sorted entry whose shifted row wraps past nb
-    while (m < tiles && (S[l][m] >> 8) < (unsigned)nb - sl[l]) m++;
-    mw[l] = m;
-    kk[l] = 0;
-    if (tiles > 0) {
-      const int m0 = m < tiles ? m : 0;
-      nm[l] = (S[l][m0] >> 8) + sl[l] - (m0 >= m ? (unsigned)nb : 0u);
-    } else {
-      nm[l] = NONE;
+    // mw: first sorted entry with v >= nb - s (binary search)
+    int lo = 0, hi = tiles;
+    const unsigned lim = (unsigned)nb - sl[l];
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if ((S2[l][mid] >> 8) < lim) lo = mid + 1;
+      else hi = mid;
     }
+    const int mw = lo;
+    // first rotated position with row >= rbeg (binary search)
+    lo = 0;
+    hi = tiles;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      const int m = mw + mid;
+      const unsigned row = (S2[l][m] >> 8) + sl[l] - (m < tiles ? (unsigned)nb : 0u);
+      if (row < (unsigned)rbeg) lo = mid + 1;
+      else hi = mid;
+    }
+    mc[l] = mw + lo;
+    me[l] = mw + tiles;
+    nm[l] = mc[l] < me[l] ? (S2[l][mc[l]] >> 8) + sl[l] - (mc[l] < tiles ? (unsigned)nb : 0u) : NONE;
     er[l] = bl[l] < residue ? ((ht.xrow[l] + sl[l]) & nbm) : NONE;
+    if (er[l] < (unsigned)rbeg) er[l] = NONE;
     re[l] = 0;
     im[l] = 0;
-  }
-  // Advance one loop's walk past the hit at row nm[l] or er[l] (whichever is
-  // smaller) and return its tap index j.
-  auto step = [&](int l) -> int {
-    int j;
-    if (er[l] < nm[l]) {
-      j = tiles;
-      er[l] = NONE;
-    } else {
-      int m = mw[l] + kk[l];
-      if (m >= tiles) m -= tiles;
-      j = (int)(S[l][m] & 255u);
-      kk[l]++;
-      if (kk[l] < tiles) {
-        const int m2 = m + 1 == tiles ? 0 : m + 1;
-        nm[l] = (S[l][m2] >> 8) + sl[l] - (m2 >= mw[l] ? (unsigned)nb : 0u);
-      } else {
-        nm[l] = NONE;
-      }
-    }
-    return j;
-  };
-  // skip the hits of earlier row groups: the rotated rows are ascending, so
-  // the first rotated position with row >= rbeg is found by binary search
-  if (rbeg > 0) {
-#pragma unroll
-    for (int l = 0; l < L; l++) {
-      int lo = 0, hi = tiles;  // first k in [0, tiles) with row(k) >= rbeg
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        int m = mw[l] + mid;
-        if (m >= tiles) m -= tiles;
-        const unsigned row = (S[l][m] >> 8) + sl[l] - (m >= mw[l] ? (unsigned)nb : 0u);
-        if (row < (unsigned)rbeg) lo = mid + 1;
-        else hi = mid;
-      }
-      kk[l] = lo;
-      if (lo < tiles) {
-        int m = mw[l] + lo;
-        if (m >= tiles) m -= tiles;
-        nm[l] = (S[l][m] >> 8) + sl[l] - (m >= mw[l] ? (unsigned)nb : 0u);
-      } else {
-        nm[l] = NONE;
-      }
-      if (er[l] < (unsigned)rbeg) er[l] = NONE;
-    }
   }
 
   const unsigned smask = (1u << logsig) - 1u;
@@ -203,20 +175,30 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     __syncthreads();
     if (abort_flag) break;
     const unsigned r0 = (unsigned)(rbeg + t * rt), r1 = r0 + (unsigned)rt;
-    // loop-major: each lane walks loop l's hits of its column inside the tile,
-    // in ascending row order
+    // Loop-major: each lane adds loop l's hits of its column inside the tile
+    // (full-tile taps in ascending row order, then the partial tap if it falls
+    // in this tile).
 #pragma unroll
     for (int l = 0; l < L; l++) {
-      while (true) {
-        const unsigned r = min(nm[l], er[l]);
-        if (r >= r1) break;
-        const V xv = tl[(r - r0) * ST + tid];
-        const int j = step(l);
-        const V f = __ldg(&filt[((size_t)j << logB) + bl[l]]);
+      while (nm[l] < r1) {
+        const unsigned ent = S2[l][mc[l]];
+        const V xv = tl[(nm[l] - r0) * ST + tid];
+        const V f = __ldg(&filt[((size_t)(ent & 255u) << logB) + bl[l]]);
         re[l] = fma(xv.x, f.x, re[l]);
         re[l] = fma(-xv.y, f.y, re[l]);
         im[l] = fma(xv.x, f.y, im[l]);
         im[l] = fma(xv.y, f.x, im[l]);
+        const int m = ++mc[l];
+        nm[l] = m < me[l] ? (S2[l][m] >> 8) + sl[l] - (m < tiles ? (unsigned)nb : 0u) : NONE;
+      }
+      if (er[l] < r1) {
+        const V xv = tl[(er[l] - r0) * ST + tid];
+        const V f = __ldg(&filt[((size_t)tiles << logB) + bl[l]]);
+        re[l] = fma(xv.x, f.x, re[l]);
+        re[l] = fma(-xv.y, f.y, re[l]);
+        im[l] = fma(xv.x, f.y, im[l]);
+        im[l] = fma(xv.y, f.x, im[l]);
+        er[l] = NONE;
       }
     }
     // RLFC sub-samples held by this tile: columns c == off (mod n/W); with
