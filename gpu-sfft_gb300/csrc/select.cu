@@ -639,6 +639,8 @@ void select_scratch_free(SelectScratch &s) {
 
 int select_launches(int key_bytes) { return key_bytes == 8 ? 9 : 6; }
 
+size_t select_state_bytes() { return sizeof(SelState); }
+
 bool g_select_coop = true;  // single-launch select when the device supports it
 
 int select_top(const void *keys, int key_bytes, long long size, const int *size_dev, int num,

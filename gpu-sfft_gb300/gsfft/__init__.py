@@ -87,6 +87,7 @@ def lib():
         "gsfft_stage_name": ([i], C.c_char_p),
         "gsfft_fft": ([P, P, ll, i, i, i, P], i),
         "gsfft_cutoff": ([P, i, i, i, i, P, P], i),
+        "gsfft_cutoff_noalloc": ([P, i, i, i, i, P, P], i),
         "gsfft_stage_perm_filter": ([i, P, i, P, i, i, i, P, i, P, P], i),
         "gsfft_stage_perm_filter_stream": ([i, P, i, P, i, i, i, P, P, P], i),
         "gsfft_stage_reverse_hash": ([P, i, P, i, i, i, i, i, i, i, u, P, P, i,
@@ -153,6 +154,18 @@ def fft(d_in, d_out, n, batch=1, sign=-1, precision=FP64, stream=0):
 def cutoff(d_samples, size, num, batch, precision, d_out, stream=0):
     check(lib().gsfft_cutoff(d_samples, size, num, batch, precision, d_out, stream or None),
           "gsfft_cutoff")
+
+
+# limits of cutoff_noalloc (GSFFT_NOALLOC_MAX_SIZE / _BATCH in gsfft.h)
+NOALLOC_MAX_SIZE = 1 << 24
+NOALLOC_MAX_BATCH = 8
+
+
+def cutoff_noalloc(d_samples, size, num, batch, precision, d_out, stream=0):
+    """gsfft_cutoff without device allocation (fixed library scratch); queued
+    on ``stream``, returns without waiting."""
+    check(lib().gsfft_cutoff_noalloc(d_samples, size, num, batch, precision, d_out,
+                                     stream or None), "gsfft_cutoff_noalloc")
 
 
 def stage_perm_filter(precision, d_x, n, d_filter_time, w, B, ai, d_bins, quirk_residue=False,

@@ -153,6 +153,25 @@ int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sig
 int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precision,
                  int *d_out, void *stream);
 
+/* No counterpart in the reference.  The same cutoff as gsfft_cutoff (same
+ * arguments, same output) for callers that must not allocate device memory
+ * while they run: a cudaMalloc/cudaFree can wait for the whole device to go
+ * idle and can fail when another allocator of the process holds the free
+ * memory.  Its scratch is one fixed device array of this library (under
+ * 1 MiB), so the call allocates nothing: at most GSFFT_NOALLOC_MAX_BATCH rows
+ * of at most GSFFT_NOALLOC_MAX_SIZE samples; larger requests return
+ * GSFFT_ERR_CAPACITY.  The work is queued on `stream` and the call returns
+ * without waiting; d_out is ready once the stream reaches that point.
+ * The first call on each device looks up the array's device address (and may
+ * load this library's device code there), so make it before any stream
+ * capture starts.  Every call on a device shares the array: calls that may
+ * overlap in time (other streams, unordered host threads) race and give
+ * undefined results; calls ordered on one stream are safe. */
+#define GSFFT_NOALLOC_MAX_SIZE (1 << 24)
+#define GSFFT_NOALLOC_MAX_BATCH 8
+int gsfft_cutoff_noalloc(const void *d_samples, int size, int num, int batch, int precision,
+                         int *d_out, void *stream);
+
 /* Stage entry points (one stage of the pipeline on caller buffers).
  * A5 (perm_filter_cutoff's first half, innerLoop.cu:194-240): bins[l*B + b]
  * for l < loops, before the bucket FFT.  d_x / d_bins hold complex_t (FP64)
