@@ -13,14 +13,16 @@
 // a bijection since a_l is odd), and tap j of that bucket sits in row
 //   r_j = (j*beta_l + s_l) mod nb,  beta_l = alpha_l^-1 mod nb,  s_l = -q_l*beta_l,
 // i.e. the column's hit rows are one per-loop set {j*beta_l mod nb} shifted by
-// s_l.  The host sorts that set once per run; each thread walks its rotated
-// copy in ascending row order, so a thread touches only its own ~loops*w/B
-// hits while the CTA streams every row of its 128 columns exactly once.
-// Sums run in ascending row (= signal position) order: fixed, no atomics.
+// s_l.  The host sorts that set once per run; a thread walks the rotated
+// copies of up to three loops of one column in ascending row order, so it
+// touches only its own ~3*w/B hits while the CTA (ceil(loops/3) threads per
+// column) streams every row of its 128 columns exactly once.  Sums run in
+// ascending row (= signal position) order: fixed, no atomics.
 //
-// Tiles of rt rows x 128 columns arrive by cp.async.bulk.tensor.2d into a
-// three-stage shared-memory ring, each stage guarded by an mbarrier whose
-// waits are bounded (a timeout sets an error flag instead of hanging).
+// Tiles of rt rows x 128 columns arrive by cp.async.bulk.tensor.2d, issued
+// by a producer warp, into a six-stage shared-memory ring guarded by full /
+// empty mbarriers whose waits are bounded (a timeout sets an error flag
+// instead of hanging).
 //
 // RLFC loop r samples positions off_r + m*(n/W) (restLocFreqCoeffKernel,
 // innerLoop.cu:693-703); (n/W) divides B, so those are whole columns and the
@@ -37,11 +39,16 @@ namespace gsfft {
 
 namespace {
 
-constexpr int ST = 128;      // columns per CTA
-constexpr int NSTAGE = 2;    // tiles in flight
+constexpr int ST = 128;      // B must be a multiple of this
+constexpr int NSTAGE = 6;    // shared-memory ring of tiles
 constexpr int MAXT = 32;     // full tiles of taps per bucket (w / B) supported
 constexpr int MAXL = 16;     // loops supported
+constexpr int PFD = 1;        // filter taps loaded ahead per thread
+constexpr int CTAS_PER_SM = 2;
 constexpr unsigned NONE = 0x7fffffffu;
+
+// columns per work item: one consumer thread per (column, loop)
+inline int cols_per_item(int loops) { return 64 * loops + 32 <= 1024 ? 64 : 32; }
 
 struct HitTab {
   unsigned s[MAXL][MAXT];  // (row offset << 8) | j, sorted by row offset
@@ -57,16 +64,50 @@ __device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned coun
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// The signal streams through L2 once; marking its tiles evict-first keeps the
+// (re-read) filter taps resident in L2 instead of being pushed out by it.
+__device__ __forceinline__ unsigned long long policy_evict_first() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ unsigned long long policy_evict_last() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
 __device__ __forceinline__ void tma_load_tile(void *dst, const CUtensorMap *tm, int x0, int y0,
-                                              unsigned long long *bar, unsigned bytes) {
+                                              unsigned long long *bar, unsigned bytes,
+                                              unsigned long long pol) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
                : "memory");
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x0), "r"(y0), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x0), "r"(y0), "r"(smem_u32(bar)), "l"(pol)
       : "memory");
+}
+
+// read-only tap load that asks L2 to keep the line
+__device__ __forceinline__ float2 ld_tap(const float2 *p, unsigned long long pol) {
+  float2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+               : "=f"(v.x), "=f"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ double2 ld_tap(const double2 *p, unsigned long long pol) {
+  double2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
 }
 
 // Bounded wait on an mbarrier phase; false after ~0.5 s without completion.
@@ -84,67 +125,118 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
   }
 }
 
-template <typename T, int L>
-__global__ void __launch_bounds__(ST, 5)
+// Persistent, warp-specialised.  A work item is (block of CW columns, row
+// group); CTA b takes items b, b + grid, ...  The last warp is the producer:
+// one lane streams every tile of the CTA's items, in order, into an NSTAGE
+// ring (full[s]: tile landed, tx-counted; empty[s]: every consumer warp is
+// done with it).  The other CW * loops threads are consumers: thread (l, col)
+// walks loop l of column col, so each warp covers 32 columns of one loop; the
+// tap of its next hit is loaded one hit ahead so the scattered L2 reads
+// overlap the stream.  No block-wide barrier inside the stream.
+template <typename T, int CW, int MAXTH>
+__global__ void __launch_bounds__(MAXTH, MAXTH <= 640 ? CTAS_PER_SM : 1)
 pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V *__restrict__ filt,
-              int logn, int logB, int w, int rt, int tiles, int rows_per_group, Draws d, HitTab ht,
-              typename Cx<T>::V *__restrict__ bins, int nrlfc, int logsig,
+              int logn, int logB, int w, int rt, int tiles, int rows_per_group, int groups, int L,
+              Draws d, HitTab ht, typename Cx<T>::V *__restrict__ bins, int nrlfc, int logsig,
               typename Cx<T>::V *__restrict__ y, int W, int *err) {
   typedef typename Cx<T>::V V;
+  constexpr int LOGCW = CW == 64 ? 6 : 5;
+  const int NCT = CW * L;  // consumer threads
+  const int NCW = NCT / 32;
   extern __shared__ __align__(128) unsigned char dsm[];
   // each loop's sorted list twice in a row, so a rotated walk needs no wrap
-  __shared__ unsigned S2[L][2 * MAXT];
-  __shared__ __align__(8) unsigned long long bar[NSTAGE];
-  __shared__ int abort_flag;
+  __shared__ unsigned S2[MAXL][2 * MAXT];
+  __shared__ unsigned s_a[MAXL], s_beta[MAXL], s_xrow[MAXL];
+  __shared__ __align__(8) unsigned long long full[NSTAGE], empty[NSTAGE];
+  __shared__ volatile int abort_flag;
   const int tid = threadIdx.x;
   const int B = 1 << logB;
   const int lognb = logn - logB;
   const int nb = 1 << lognb;
   const unsigned nbm = (unsigned)nb - 1u;
   const unsigned nmask = (1u << logn) - 1u;
-  const int c0 = blockIdx.x * ST;
-  const unsigned c = (unsigned)(c0 + tid);
-  const unsigned stage_bytes = (unsigned)(rt * ST * sizeof(V));
-  const int rbeg = blockIdx.y * rows_per_group;  // this CTA's rows: [rbeg, rbeg + rows_per_group)
+  const unsigned stage_bytes = (unsigned)(rt * CW * sizeof(V));
   const int ntile = rows_per_group / rt;
+  const int ncb = B / CW;
+  const int items = ncb * groups;
   const int xmul = (int)(sizeof(V) / 8);  // tensor elements are 8-byte words
   V *tile0 = reinterpret_cast<V *>(dsm);
 
-  for (int e = tid; e < L * 2 * MAXT; e += ST) {
+  for (int e = tid; e < L * 2 * MAXT; e += blockDim.x) {
     const int l = e / (2 * MAXT), m = e % (2 * MAXT);
     S2[l][m] = m < tiles ? ht.s[l][m] : (m < 2 * tiles ? ht.s[l][m - tiles] : 0u);
   }
+  if (tid < L) {
+    s_a[tid] = (unsigned)d.a[tid];
+    s_beta[tid] = ht.beta[tid];
+    s_xrow[tid] = ht.xrow[tid];
+  }
   if (tid == 0) {
     abort_flag = 0;
-    for (int s = 0; s < NSTAGE; s++) mbar_init(&bar[s], 1);
+    for (int s = 0; s < NSTAGE; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], NCW);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0)
-    for (int t = 0; t < NSTAGE && t < ntile; t++)
-      tma_load_tile(reinterpret_cast<char *>(tile0) + (size_t)t * stage_bytes, &tmap, c0 * xmul,
-                    rbeg + t * rt, &bar[t], stage_bytes);
 
-  // Walk state per loop.  Rotated position k of the column's hit list is
-  // doubled-list entry m = mw + k; its row is v + s - nb when m < tiles (the
-  // entry wrapped past nb) and v + s otherwise.
+  if (tid >= NCT) {
+    // ---------------- producer
+    if (tid == NCT) {
+      const unsigned long long pol = policy_evict_first();
+      long long k = 0;
+      bool ok = true;
+      for (int it = blockIdx.x; it < items && ok; it += gridDim.x) {
+        const int cb = it % ncb, g = it / ncb;
+        for (int t = 0; t < ntile; t++, k++) {
+          const int st = (int)(k % NSTAGE);
+          if (!mbar_wait(&empty[st], (unsigned)((k / NSTAGE) & 1) ^ 1u) || abort_flag) {
+            abort_flag = 1;
+            ok = false;
+            break;
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          tma_load_tile(reinterpret_cast<char *>(tile0) + (size_t)st * stage_bytes, &tmap,
+                        cb * CW * xmul, g * rows_per_group + t * rt, &full[st], stage_bytes, pol);
+        }
+      }
+      // stay until the last load of every stage has landed (bounded)
+      for (long long j = k - NSTAGE < 0 ? 0 : k - NSTAGE; j < k; j++)
+        if (!mbar_wait(&full[j % NSTAGE], (unsigned)((j / NSTAGE) & 1))) {
+          atomicExch(err, 1);
+          break;
+        }
+    }
+    return;
+  }
+
+  // ---------------- consumers
+  const int col = tid & (CW - 1), l = tid >> LOGCW, lane = tid & 31;
   const int residue = w & (B - 1);
-  int bl[L], mc[L], me[L];
-  unsigned sl[L], nm[L], er[L];
-  T re[L], im[L];
-#pragma unroll
-  for (int l = 0; l < L; l++) {
-    const unsigned a = (unsigned)d.a[l];
+  const unsigned smask = (1u << logsig) - 1u;
+  const unsigned a = s_a[l], beta = s_beta[l], xrow = s_xrow[l];
+  const unsigned *S = S2[l];
+  const unsigned long long keep = policy_evict_last();
+  long long k = 0;
+  for (int it = blockIdx.x; it < items; it += gridDim.x) {
+    const int cb = it % ncb, g = it / ncb;
+    const int c0 = cb * CW;
+    const unsigned c = (unsigned)(c0 + col);
+    const int rbeg = g * rows_per_group;
+    // Walk state.  Rotated position k of the column's hit list is
+    // doubled-list entry m = mw + k; its row is v + s - nb when m < tiles (the
+    // entry wrapped past nb) and v + s otherwise.
     const unsigned prod = c * a;
-    bl[l] = (int)(prod & (unsigned)(B - 1));
+    const int bl = (int)(prod & (unsigned)(B - 1));
     const unsigned q = (prod & nmask) >> logB;
-    sl[l] = (0u - q * ht.beta[l]) & nbm;
+    const unsigned sl = (0u - q * beta) & nbm;
     // mw: first sorted entry with v >= nb - s (binary search)
     int lo = 0, hi = tiles;
-    const unsigned lim = (unsigned)nb - sl[l];
+    const unsigned lim = (unsigned)nb - sl;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if ((S2[l][mid] >> 8) < lim) lo = mid + 1;
+      if ((S[mid] >> 8) < lim) lo = mid + 1;
       else hi = mid;
     }
     const int mw = lo;
@@ -154,86 +246,83 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
       const int m = mw + mid;
-      const unsigned row = (S2[l][m] >> 8) + sl[l] - (m < tiles ? (unsigned)nb : 0u);
+      const unsigned row = (S[m] >> 8) + sl - (m < tiles ? (unsigned)nb : 0u);
       if (row < (unsigned)rbeg) lo = mid + 1;
       else hi = mid;
     }
-    mc[l] = mw + lo;
-    me[l] = mw + tiles;
-    nm[l] = mc[l] < me[l] ? (S2[l][mc[l]] >> 8) + sl[l] - (mc[l] < tiles ? (unsigned)nb : 0u) : NONE;
-    er[l] = bl[l] < residue ? ((ht.xrow[l] + sl[l]) & nbm) : NONE;
-    if (er[l] < (unsigned)rbeg) er[l] = NONE;
-    re[l] = 0;
-    im[l] = 0;
-  }
+    int mc = mw + lo;
+    const int me = mw + tiles;
+    const V *fcol = filt + bl;
+    unsigned nm = NONE, er = NONE;
+    // taps of the next PFD hits, loaded ahead (the last entries of the
+    // doubled list are valid indices, so loading past me is harmless)
+    V fv[PFD];
+#pragma unroll
+    for (int u = 0; u < PFD; u++)
+      fv[u] = ld_tap(fcol + ((size_t)(S[min(mc + u, 2 * tiles - 1)] & 255u) << logB), keep);
+    V fe = mk((T)0, (T)0);
+    if (mc < me) {
+      const unsigned ent = S[mc];
+      nm = (ent >> 8) + sl - (mc < tiles ? (unsigned)nb : 0u);
+    }
+    if (bl < residue) {
+      er = (xrow + sl) & nbm;
+      if (er < (unsigned)rbeg) er = NONE;
+      else fe = ld_tap(fcol + ((size_t)tiles << logB), keep);
+    }
+    T re = 0, im = 0;
 
-  const unsigned smask = (1u << logsig) - 1u;
-  for (int t = 0; t < ntile; t++) {
-    const int st = t % NSTAGE;
-    const V *tl = tile0 + (size_t)st * rt * ST;
-    if (tid == 0 && !mbar_wait(&bar[st], (unsigned)(t / NSTAGE) & 1u)) abort_flag = 1;
-    __syncthreads();
-    if (abort_flag) break;
-    const unsigned r0 = (unsigned)(rbeg + t * rt), r1 = r0 + (unsigned)rt;
-    // Loop-major: each lane adds loop l's hits of its column inside the tile
-    // (full-tile taps in ascending row order, then the partial tap if it falls
-    // in this tile).
+    for (int t = 0; t < ntile; t++, k++) {
+      const int st = (int)(k % NSTAGE);
+      const V *tl = tile0 + (size_t)st * rt * CW;
+      if (!mbar_wait(&full[st], (unsigned)((k / NSTAGE) & 1))) {
+        abort_flag = 1;
+        atomicExch(err, 1);
+        return;
+      }
+      const unsigned r0 = (unsigned)(rbeg + t * rt), r1 = r0 + (unsigned)rt;
+      // full-tile taps in ascending row order, then the partial tap if it
+      // falls in this tile
+      while (nm < r1) {
+        const V xv = tl[((nm - r0) << LOGCW) + col];
+        re = fma(xv.x, fv[0].x, re);
+        re = fma(-xv.y, fv[0].y, re);
+        im = fma(xv.x, fv[0].y, im);
+        im = fma(xv.y, fv[0].x, im);
 #pragma unroll
-    for (int l = 0; l < L; l++) {
-      while (nm[l] < r1) {
-        const unsigned ent = S2[l][mc[l]];
-        const V xv = tl[(nm[l] - r0) * ST + tid];
-        const V f = __ldg(&filt[((size_t)(ent & 255u) << logB) + bl[l]]);
-        re[l] = fma(xv.x, f.x, re[l]);
-        re[l] = fma(-xv.y, f.y, re[l]);
-        im[l] = fma(xv.x, f.y, im[l]);
-        im[l] = fma(xv.y, f.x, im[l]);
-        const int m = ++mc[l];
-        nm[l] = m < me[l] ? (S2[l][m] >> 8) + sl[l] - (m < tiles ? (unsigned)nb : 0u) : NONE;
+        for (int u = 0; u + 1 < PFD; u++) fv[u] = fv[u + 1];
+        const int m = ++mc;
+        fv[PFD - 1] = ld_tap(fcol + ((size_t)(S[min(m + PFD - 1, 2 * tiles - 1)] & 255u) << logB), keep);
+        nm = m < me ? (S[m] >> 8) + sl - (m < tiles ? (unsigned)nb : 0u) : NONE;
       }
-      if (er[l] < r1) {
-        const V xv = tl[(er[l] - r0) * ST + tid];
-        const V f = __ldg(&filt[((size_t)tiles << logB) + bl[l]]);
-        re[l] = fma(xv.x, f.x, re[l]);
-        re[l] = fma(-xv.y, f.y, re[l]);
-        im[l] = fma(xv.x, f.y, im[l]);
-        im[l] = fma(xv.y, f.x, im[l]);
-        er[l] = NONE;
+      if (er < r1) {
+        const V xv = tl[((er - r0) << LOGCW) + col];
+        re = fma(xv.x, fe.x, re);
+        re = fma(-xv.y, fe.y, re);
+        im = fma(xv.x, fe.y, im);
+        im = fma(xv.y, fe.x, im);
+        er = NONE;
       }
-    }
-    // RLFC sub-samples held by this tile: columns c == off (mod n/W); with
-    // n/W <= 128 there are 128 >> logsig of them, else at most one
-    for (int rr = 0; rr < nrlfc; rr++) {
-      const unsigned off = (unsigned)d.offs[rr];
-      const unsigned first = ((off - (unsigned)c0) & smask);  // first matching column index
-      if (first >= (unsigned)ST) continue;
-      const int lognc = logsig >= 7 ? 0 : 7 - logsig;         // log2 of the column count
-      for (int e = tid; e < (rt << lognc); e += ST) {
-        const int row = e >> lognc, ci = e & ((1 << lognc) - 1);
-        const unsigned cc = first + ((unsigned)ci << logsig);
-        const unsigned tpos = ((r0 + row) << logB) + (unsigned)c0 + cc;
-        y[(size_t)rr * W + ((tpos - off) >> logsig)] = tl[row * ST + cc];
+      // RLFC sub-samples held by this tile: columns c == off (mod n/W); with
+      // n/W <= CW there are CW >> logsig of them, else at most one
+      for (int rr = 0; rr < nrlfc; rr++) {
+        const unsigned off = (unsigned)d.offs[rr];
+        const unsigned first = ((off - (unsigned)c0) & smask);  // first matching column index
+        if (first >= (unsigned)CW) continue;
+        const int lognc = logsig >= LOGCW ? 0 : LOGCW - logsig;  // log2 of the column count
+        for (int e = tid; e < (rt << lognc); e += NCT) {
+          const int row = e >> lognc, ci = e & ((1 << lognc) - 1);
+          const unsigned cc = first + ((unsigned)ci << logsig);
+          const unsigned tpos = ((r0 + row) << logB) + (unsigned)c0 + cc;
+          y[(size_t)rr * W + ((tpos - off) >> logsig)] = tl[(row << LOGCW) + cc];
+        }
       }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);
     }
-    __syncthreads();  // every thread is done with stage st
-    if (tid == 0 && t + NSTAGE < ntile) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tma_load_tile(reinterpret_cast<char *>(tile0) + (size_t)st * stage_bytes, &tmap, c0 * xmul,
-                    rbeg + (t + NSTAGE) * rt, &bar[st], stage_bytes);
-    }
+    // partial sums of this row group: bins[group][l][b]
+    bins[((size_t)g * L + l) * B + bl] = mk(re, im);
   }
-  if (abort_flag) {
-    // drain: wait (bounded) for any copy still in flight into this CTA
-    if (tid == 0) {
-      for (int s = 0; s < NSTAGE; s++) (void)mbar_wait(&bar[s], 0);
-      atomicExch(err, 1);
-    }
-    return;
-  }
-  // partial sums of this row group: bins[group][l][b]
-  V *part = bins + (size_t)blockIdx.y * L * B;
-#pragma unroll
-  for (int l = 0; l < L; l++) part[(size_t)l * B + bl[l]] = mk(re[l], im[l]);
 }
 
 template <typename V>
@@ -270,23 +359,31 @@ unsigned inv_odd(unsigned a) {  // a^-1 mod 2^32 for odd a (Newton)
   return x;
 }
 
-template <typename T, int L>
-int launch_L(const CUtensorMap &tm, const void *filt, int logn, int logB, int w, int rt, int tiles,
-             int groups, const Draws &d, const HitTab &ht, void *bins, int nrlfc, int logsig, void *y,
-             int W, int *err, cudaStream_t st) {
+template <typename T, int CW, int MAXTH>
+int launch_CW(const CUtensorMap &tm, const void *filt, int logn, int logB, int w, int rt, int tiles,
+              int groups, int loops, const Draws &d, const HitTab &ht, void *bins, int nrlfc,
+              int logsig, void *y, int W, int *err, cudaStream_t st) {
   typedef typename Cx<T>::V V;
   const int B = 1 << logB;
-  const int smem = NSTAGE * rt * ST * (int)sizeof(V);
-  static bool attr = false;
-  if (!attr) {
-    GS_CUDA(cudaFuncSetAttribute(pf_tma_kernel<T, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem));
-    attr = true;
+  const int smem = NSTAGE * rt * CW * (int)sizeof(V);
+  const int threads = CW * loops + 32;
+  static int attr = 0;
+  if (attr < smem) {
+    GS_CUDA(cudaFuncSetAttribute(pf_tma_kernel<T, CW, MAXTH>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = smem;
   }
+  int dev = 0, sms = 0, per_sm = 0;
+  GS_CUDA(cudaGetDevice(&dev));
+  GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pf_tma_kernel<T, CW, MAXTH>,
+                                                        threads, smem));
+  const int items = (B / CW) * groups;
+  const int grid = std::max(1, std::min(items, std::max(per_sm, 1) * sms));
   const int rows_per_group = (1 << (logn - logB)) / groups;
-  pf_tma_kernel<T, L><<<dim3(B / ST, groups), ST, smem, st>>>(tm, (const V *)filt, logn, logB, w, rt,
-                                                              tiles, rows_per_group, d, ht, (V *)bins,
-                                                              nrlfc, logsig, (V *)y, W, err);
+  pf_tma_kernel<T, CW, MAXTH><<<grid, threads, smem, st>>>(
+      tm, (const V *)filt, logn, logB, w, rt, tiles, rows_per_group, groups, loops, d, ht, (V *)bins,
+      nrlfc, logsig, (V *)y, W, err);
   return GSFFT_OK;
 }
 
@@ -294,13 +391,18 @@ template <typename T>
 int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int logB, int w, int rt,
              int tiles, int groups, const Draws &d, const HitTab &ht, void *bins, int nrlfc,
              int logsig, void *y, int W, int *err, cudaStream_t st) {
-  switch (loops) {
-#define C(LL) \
-  case LL: return launch_L<T, LL>(tm, filt, logn, logB, w, rt, tiles, groups, d, ht, bins, nrlfc, logsig, y, W, err, st);
-    C(2) C(3) C(4) C(5) C(6) C(7) C(8) C(9) C(10) C(11) C(12) C(13) C(14) C(15) C(16)
-#undef C
-    default: return GSFFT_ERR_UNSUPPORTED;
+  const int cw = cols_per_item(loops);
+  const bool small = cw * loops + 32 <= 640;
+#define GO(CWV, MT)                                                                                \
+  return launch_CW<T, CWV, MT>(tm, filt, logn, logB, w, rt, tiles, groups, loops, d, ht, bins, nrlfc, \
+                               logsig, y, W, err, st)
+  if (cw == 64) {
+    if (small) GO(64, 640);
+    GO(64, 1024);
   }
+  if (small) GO(32, 640);
+  GO(32, 1024);
+#undef GO
 }
 
 }  // namespace
@@ -325,13 +427,22 @@ bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops) {
   return encode_fn() != nullptr;
 }
 
-int stream_pf_groups(int n, int B, int precision) {
+static int stream_rows_per_tile(int n, int B, int precision) {
+  return std::min(n / B, precision == GSFFT_FP64 ? 16 : 32);  // 16 KiB tiles of 64 columns
+}
+
+int stream_pf_groups(int n, int B, int loops, int precision) {
   const int nb = n / B;
-  const int rt = std::min(nb, precision == GSFFT_FP64 ? 8 : 16);
-  // at least ~2400 CTAs (several waves of ~5 resident CTAs on 152 SMs), each
-  // group at least one tile
+  const int rt = stream_rows_per_tile(n, B, precision);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // enough work items (column block x row group) for ~6 per persistent CTA,
+  // each item at least four tiles long
+  const long long want = 6LL * CTAS_PER_SM * sms;
+  const int cw = cols_per_item(loops);
   int groups = 1;
-  while ((long long)(B / ST) * groups < 1500 && nb / (groups * 2) >= rt) groups *= 2;
+  while ((long long)(B / cw) * groups < want && nb / (groups * 2) >= 4 * rt) groups *= 2;
   return groups;
 }
 
@@ -360,12 +471,13 @@ int launch_perm_filter_stream(int precision, const void *x, int n, const void *f
   // x as a 2-D tensor of 8-byte words: nb rows of B (FP32) or 2B (FP64) words
   const bool dbl = precision == GSFFT_FP64;
   const int es = dbl ? 16 : 8;
-  const int rt = std::min(nb, dbl ? 8 : 16);
-  const int groups = stream_pf_groups(n, B, precision);
+  const int rt = stream_rows_per_tile(n, B, precision);
+  const int groups = stream_pf_groups(n, B, loops, precision);
+  const int cw = cols_per_item(loops);
   CUtensorMap tm;
   const cuuint64_t gdim[2] = {(cuuint64_t)B * (es / 8), (cuuint64_t)nb};
   const cuuint64_t gstride[1] = {(cuuint64_t)B * es};
-  const cuuint32_t box[2] = {(cuuint32_t)(ST * (es / 8)), (cuuint32_t)rt};
+  const cuuint32_t box[2] = {(cuuint32_t)(cw * (es / 8)), (cuuint32_t)rt};
   const cuuint32_t estr[2] = {1, 1};
   CUresult cr = encode_fn()(&tm, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<void *>(x), gdim,
                             gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,

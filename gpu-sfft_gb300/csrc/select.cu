@@ -347,20 +347,29 @@ int select_impl(const void *keys, long long size, const int *size_dev, int num, 
 
 
 // ---------------------------------------------------------------------------
-// Single-launch form: the same passes in one cooperative kernel separated by
-// grid-wide syncs.  Every CTA re-derives the digit of each row from the shared
-// histogram, so one sync per pass suffices.  Histograms are left zeroed for
-// the next call.
+// Single-launch form: the same selection in one cooperative kernel.  Row b
+// is split into `cpr` contiguous chunks, one per CTA.  Each radix pass builds
+// the CTA's chunk histogram in shared memory and adds it to the row's global
+// histogram once; after a grid-wide sync every CTA derives its row's digit
+// itself.  A pass ends the descent early when the threshold's bin is "pure":
+// it holds one sample, or it is the first pass's digit 0 while the rounding
+// floor maps every key of that digit to exact zero.  Keys are then compared
+// on the bits decided so far.  Counting and writing use per-thread runs of
+// contiguous samples and one packed block scan per sub-tile, so ids come out
+// ascending.  Histograms are left zeroed for the next call.
 // ---------------------------------------------------------------------------
 namespace cg = cooperative_groups;
 
-constexpr int MAXB = 8;  // rows per cooperative call
+constexpr int MAXB = 8;         // rows per cooperative call
+constexpr int CT = 512;         // threads per CTA
+constexpr int SPT = 8;          // contiguous samples per thread in the write pass
+constexpr int CHUNK_MIN = 8192; // smallest chunk per CTA
 
 struct CoopArgs {
   const void *keys;
   long long size;        // capacity per row
   const int *size_dev;   // live size (batch 1) or null
-  int num, batch;
+  int num, batch, cpr;
   long long row_stride;
   int *out;
   long long out_stride;
@@ -368,78 +377,95 @@ struct CoopArgs {
   const void *row_max;
   double floor_rel;
   unsigned *hist;        // [6][MAXB][HIST_BINS], zero on entry and on exit
-  unsigned *tiles;       // [MAXB][max_tiles][2]
+  unsigned *tiles;       // [MAXB][max_tiles][2]: per-chunk (#greater, #equal)
   int max_tiles;
 };
 
-struct RowSt {
-  unsigned long long floor, prefix;
-  long long rank;
-  int size, take_all;
-};
+// Block-wide exclusive scan over CT threads (two syncs).
+__device__ __forceinline__ unsigned ct_excl_scan(unsigned v, unsigned *ws, unsigned *total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned w = lane < CT / 32 ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < CT / 32) ws[lane] = w;
+  }
+  __syncthreads();
+  const unsigned base = wid ? ws[wid - 1] : 0;
+  const unsigned tot = ws[CT / 32 - 1];
+  __syncthreads();
+  if (total) *total = tot;
+  return base + x - v;
+}
 
 template <typename K>
-__global__ void __launch_bounds__(SEL_THREADS) sel_coop_kernel(CoopArgs a) {
+__global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
   cg::grid_group grid = cg::this_grid();
   __shared__ unsigned sh[HIST_BINS];
-  __shared__ unsigned warp_sums[SEL_THREADS / 32];
-  __shared__ RowSt rs[MAXB];
+  __shared__ unsigned ws[CT / 32];
+  __shared__ unsigned long long s_prefix;
+  __shared__ long long s_rank;
+  __shared__ unsigned s_bincount;
   const int tid = threadIdx.x, lane = tid & 31;
   const int kb = (int)sizeof(K) * 8;
   const int w64[6] = {11, 11, 11, 11, 10, 10};
   const int w32[3] = {11, 11, 10};
   const int npass = kb == 64 ? 6 : 3;
-  if (tid < a.batch) {
-    const int b = tid;
-    long long sz = a.size;
-    if (a.size_dev) {
-      long long dv = *a.size_dev;
-      sz = dv < a.size ? dv : a.size;
-      if (sz < 0) sz = 0;
-    }
-    RowSt r;
-    r.floor = 0;
-    if (a.row_max && a.floor_rel > 0.0) {
-      if (kb == 64) {
-        const double m = __longlong_as_double((long long)reinterpret_cast<const unsigned long long *>(a.row_max)[b]);
-        r.floor = (unsigned long long)__double_as_longlong(m * a.floor_rel);
-      } else {
-        const float m = __uint_as_float(reinterpret_cast<const unsigned *>(a.row_max)[b]);
-        r.floor = __float_as_uint((float)((double)m * a.floor_rel));
-      }
-    }
-    r.prefix = 0;
-    r.size = (int)sz;
-    r.take_all = sz <= a.num ? 1 : 0;
-    r.rank = sz - a.num - 1;
-    rs[b] = r;
+  const int b = blockIdx.x / a.cpr, ci = blockIdx.x % a.cpr;
+  // row state (identical in every CTA of the row)
+  long long sz = a.size;
+  if (a.size_dev) {
+    const long long dv = *a.size_dev;
+    sz = dv < a.size ? dv : a.size;
+    if (sz < 0) sz = 0;
   }
-  __syncthreads();
-  const int T = (int)((a.size + SEL_TILE - 1) / SEL_TILE);
-  const int nitems = a.batch * T;
+  K floor = 0;
+  if (a.row_max && a.floor_rel > 0.0) {
+    if (kb == 64) {
+      const double m = __longlong_as_double((long long)reinterpret_cast<const unsigned long long *>(a.row_max)[b]);
+      floor = (K)(unsigned long long)__double_as_longlong(m * a.floor_rel);
+    } else {
+      const float m = __uint_as_float(reinterpret_cast<const unsigned *>(a.row_max)[b]);
+      floor = (K)__float_as_uint((float)((double)m * a.floor_rel));
+    }
+  }
+  const bool take_all = sz <= a.num;
+  const long long chunk = ((sz + a.cpr - 1) / a.cpr + 31) & ~31LL;
+  const long long lo = (long long)ci * chunk < sz ? (long long)ci * chunk : sz;
+  const long long hi = lo + chunk < sz ? lo + chunk : sz;
+  const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
+  unsigned long long prefix = 0;
+  long long rank = sz - a.num - 1;
+  int cmp_shift = 0;  // low bits ignored by the final comparisons
+  bool done = take_all;
   int shift = kb;
   for (int p = 0; p < npass; p++) {
     const int width = kb == 64 ? w64[p] : w32[p];
     shift -= width;
-    const unsigned dmask = (1u << width) - 1u;
-    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-      const int b = it / T, tile = it - b * T;
-      const RowSt r = rs[b];
-      if (r.take_all || (long long)tile * SEL_TILE >= r.size) continue;
-      for (int i = tid; i < HIST_BINS; i += SEL_THREADS) sh[i] = 0;
-      __syncthreads();
+    if (!done) {
+      const unsigned dmask = (1u << width) - 1u;
       const unsigned long long hi_mask =
           (shift + width >= kb) ? 0ull : (~0ull << (shift + width)) & (kb == 64 ? ~0ull : 0xffffffffull);
-      const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
-      const long long base = (long long)tile * SEL_TILE;
-#pragma unroll 4
-      for (int q = 0; q < SEL_ITEMS; q++) {
-        const long long i = base + q * SEL_THREADS + tid;
+      for (int i = tid; i < HIST_BINS; i += CT) sh[i] = 0;
+      __syncthreads();
+      for (long long base = lo; base < hi; base += CT) {
+        const long long i = base + tid;
         bool hit = false;
         unsigned digit = 0;
-        if (i < r.size) {
-          const unsigned long long k = (unsigned long long)load_key<K>(row, i, (K)r.floor);
-          hit = (k & hi_mask) == r.prefix;
+        if (i < hi) {
+          const unsigned long long k = (unsigned long long)load_key<K>(row, i, floor);
+          hit = (k & hi_mask) == prefix;
           digit = (unsigned)(k >> shift) & dmask;
         }
         const unsigned key = hit ? digit : (0x80000000u | (unsigned)lane);
@@ -448,17 +474,15 @@ __global__ void __launch_bounds__(SEL_THREADS) sel_coop_kernel(CoopArgs a) {
       }
       __syncthreads();
       unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
-      for (int i = tid; i < HIST_BINS; i += SEL_THREADS)
+      for (int i = tid; i < HIST_BINS; i += CT)
         if (sh[i]) atomicAdd(&gh[i], sh[i]);
-      __syncthreads();
     }
     grid.sync();
-    // every CTA finds the digit of each row holding its remaining rank
-    for (int b = 0; b < a.batch; b++) {
-      if (rs[b].take_all) continue;
+    if (!done) {
+      // the digit holding ascending rank `rank` of this row
       const unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
-      const int per = HIST_BINS / SEL_THREADS;
-      unsigned local[HIST_BINS / SEL_THREADS];
+      constexpr int per = HIST_BINS / CT;
+      unsigned local[per];
       unsigned sum = 0;
 #pragma unroll
       for (int q = 0; q < per; q++) {
@@ -466,106 +490,109 @@ __global__ void __launch_bounds__(SEL_THREADS) sel_coop_kernel(CoopArgs a) {
         sum += local[q];
       }
       unsigned tot;
-      const unsigned before = block_excl_scan(sum, warp_sums, &tot);
-      const long long rank = rs[b].rank;
-      const unsigned long long prefix = rs[b].prefix;
-      __syncthreads();
+      const unsigned before = ct_excl_scan(sum, ws, &tot);
       unsigned run = before;
 #pragma unroll
       for (int q = 0; q < per; q++) {
         if ((long long)run <= rank && rank < (long long)run + local[q]) {
-          rs[b].prefix = prefix | ((unsigned long long)(tid * per + q) << shift);
-          rs[b].rank = rank - run;
+          s_prefix = prefix | ((unsigned long long)(tid * per + q) << shift);
+          s_rank = rank - run;
+          s_bincount = local[q];
         }
         run += local[q];
       }
       __syncthreads();
+      prefix = s_prefix;
+      rank = s_rank;
+      const unsigned cnt = s_bincount;
+      __syncthreads();
+      const bool zero_bin = p == 0 && (prefix >> shift) == 0 && (unsigned long long)floor >= (1ull << shift);
+      if (cnt == 1) {
+        cmp_shift = shift;
+        done = true;
+      } else if (zero_bin) {
+        done = true;  // every key of the bin was floored to exactly 0
+      }
+      if (p == npass - 1) done = true;
     }
   }
-  // counting pass
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const int b = it / T, tile = it - b * T;
-    const RowSt r = rs[b];
-    if (r.take_all) continue;
-    const K thr = (K)r.prefix;
-    const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
-    const long long base = (long long)tile * SEL_TILE;
-    unsigned gt = 0, eq = 0;
-    if (base < r.size) {
-#pragma unroll 4
-      for (int q = 0; q < SEL_ITEMS; q++) {
-        const long long i = base + q * SEL_THREADS + tid;
-        if (i < r.size) {
-          const K k = load_key<K>(row, i, (K)r.floor);
-          gt += k > thr;
-          eq += k == thr;
-        }
-      }
+  // counting pass: (#greater, #equal) of this chunk
+  const K thr = (K)prefix;
+  const unsigned long long thr_c = (unsigned long long)thr >> cmp_shift;
+  unsigned gt = 0, eq = 0;
+  if (!take_all) {
+    for (long long i = lo + tid; i < hi; i += CT) {
+      const unsigned long long kc = (unsigned long long)load_key<K>(row, i, floor) >> cmp_shift;
+      gt += kc > thr_c;
+      eq += kc == thr_c;
     }
-    unsigned tgt, teq;
-    block_excl_scan(gt, warp_sums, &tgt);
-    block_excl_scan(eq, warp_sums, &teq);
-    if (tid == 0) {
-      a.tiles[((size_t)b * a.max_tiles + tile) * 2 + 0] = tgt;
-      a.tiles[((size_t)b * a.max_tiles + tile) * 2 + 1] = teq;
-    }
+  }
+  unsigned tgt, teq;
+  ct_excl_scan(gt, ws, &tgt);
+  ct_excl_scan(eq, ws, &teq);
+  if (tid == 0) {
+    a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 0] = tgt;
+    a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = teq;
   }
   grid.sync();
   // every CTA has read the histograms: zero them for the next call
-  for (int i = blockIdx.x * SEL_THREADS + tid; i < npass * MAXB * HIST_BINS; i += gridDim.x * SEL_THREADS)
+  for (long long i = (long long)blockIdx.x * CT + tid; i < (long long)npass * MAXB * HIST_BINS;
+       i += (long long)gridDim.x * CT)
     a.hist[i] = 0;
   // writing pass
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const int b = it / T, tile = it - b * T;
-    const RowSt r = rs[b];
-    int *o = a.out + (size_t)b * a.out_stride;
-    const long long base = (long long)tile * SEL_TILE;
-    if (r.take_all) {
-      for (int q = 0; q < SEL_ITEMS; q++) {
-        const long long i = base + q * SEL_THREADS + tid;
-        if (i < r.size) o[i] = (int)i;
-      }
-      continue;
-    }
-    if (base >= r.size) continue;
-    // prefix of this tile and totals of the row
+  int *o = a.out + (size_t)b * a.out_stride;
+  if (take_all) {
+    for (long long i = lo + tid; i < hi; i += CT) o[i] = (int)i;
+  } else {
+    // chunk prefix and row totals
     unsigned bg = 0, be = 0, tg = 0;
     const unsigned *tb = a.tiles + (size_t)b * a.max_tiles * 2;
-    for (int t2 = tid; t2 < T; t2 += SEL_THREADS) {
-      const unsigned vg = __ldcg(&tb[t2 * 2]), ve = __ldcg(&tb[t2 * 2 + 1]);
-      if (t2 < tile) { bg += vg; be += ve; }
+    for (int c2 = tid; c2 < a.cpr; c2 += CT) {
+      const unsigned vg = __ldcg(&tb[c2 * 2]), ve = __ldcg(&tb[c2 * 2 + 1]);
+      if (c2 < ci) {
+        bg += vg;
+        be += ve;
+      }
       tg += vg;
     }
     unsigned s_bg, s_be, s_tg;
-    block_excl_scan(bg, warp_sums, &s_bg);
-    block_excl_scan(be, warp_sums, &s_be);
-    block_excl_scan(tg, warp_sums, &s_tg);
+    ct_excl_scan(bg, ws, &s_bg);
+    ct_excl_scan(be, ws, &s_be);
+    ct_excl_scan(tg, ws, &s_tg);
     const unsigned need_eq = (unsigned)(a.num - (int)s_tg);
     unsigned gt_run = s_bg, eq_run = s_be;
-    const K thr = (K)r.prefix;
-    const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
-    for (int q = 0; q < SEL_ITEMS; q++) {
-      const long long i = base + q * SEL_THREADS + tid;
-      unsigned g = 0, e = 0;
-      if (i < r.size) {
-        const K k = load_key<K>(row, i, (K)r.floor);
-        g = k > thr;
-        e = k == thr;
+    for (long long base = lo; base < hi; base += (long long)CT * SPT) {
+      const long long i0 = base + (long long)tid * SPT;
+      unsigned flags = 0, ng = 0, ne = 0;  // bit 2q: greater, bit 2q+1: equal
+#pragma unroll
+      for (int q = 0; q < SPT; q++) {
+        const long long i = i0 + q;
+        if (i < hi) {
+          const unsigned long long kc = (unsigned long long)load_key<K>(row, i, floor) >> cmp_shift;
+          const unsigned g = kc > thr_c, e = kc == thr_c;
+          flags |= (g << (2 * q)) | (e << (2 * q + 1));
+          ng += g;
+          ne += e;
+        }
       }
-      unsigned cg_, ce;
-      const unsigned pg = block_excl_scan(g, warp_sums, &cg_);
-      const unsigned pe = block_excl_scan(e, warp_sums, &ce);
-      const unsigned eq_before = eq_run + pe;
-      if (g || (e && eq_before < need_eq)) {
-        const unsigned pos = gt_run + pg + (eq_before < need_eq ? eq_before : need_eq);
-        if (pos < (unsigned)a.num) o[pos] = (int)i;
+      unsigned tot;
+      const unsigned pre = ct_excl_scan(ng | (ne << 16), ws, &tot);
+      unsigned gb = gt_run + (pre & 0xffffu), eb = eq_run + (pre >> 16);
+#pragma unroll
+      for (int q = 0; q < SPT; q++) {
+        const unsigned g = (flags >> (2 * q)) & 1u, e = (flags >> (2 * q + 1)) & 1u;
+        if (g || (e && eb < need_eq)) {
+          const unsigned pos = gb + (eb < need_eq ? eb : need_eq);
+          if (pos < (unsigned)a.num) o[pos] = (int)(i0 + q);
+        }
+        gb += g;
+        eb += e;
       }
-      gt_run += cg_;
-      eq_run += ce;
+      gt_run += tot & 0xffffu;
+      eq_run += tot >> 16;
     }
   }
-  if (a.count_out && blockIdx.x == 0 && tid < a.batch)
-    a.count_out[tid] = rs[tid].take_all ? rs[tid].size : a.num;
+  if (a.count_out && ci == 0 && tid == 0) a.count_out[b] = take_all ? (int)sz : a.num;
 }
 
 template <typename K>
@@ -577,7 +604,7 @@ int coop_grid() {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (!coop) return -1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K>, SEL_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K>, CT, 0);
     g = per > 0 ? per * sms : -1;
   }
   return g;
@@ -587,15 +614,19 @@ template <typename K>
 int select_coop_impl(const void *keys, long long size, const int *size_dev, int num, int batch,
                      long long row_stride, int *out, long long out_stride, int *count_out,
                      SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
-  const long long tiles = (size + SEL_TILE - 1) / SEL_TILE;
   const int maxg = coop_grid<K>();
   if (maxg <= 0) return GSFFT_ERR_UNSUPPORTED;
+  long long cpr = (size + CHUNK_MIN - 1) / CHUNK_MIN;
+  if (cpr > maxg / batch) cpr = maxg / batch;
+  if (cpr > s.max_tiles) cpr = s.max_tiles;
+  if (cpr < 1) return GSFFT_ERR_UNSUPPORTED;
   CoopArgs a;
   a.keys = keys;
   a.size = size;
   a.size_dev = size_dev;
   a.num = num;
   a.batch = batch;
+  a.cpr = (int)cpr;
   a.row_stride = row_stride;
   a.out = out;
   a.out_stride = out_stride;
@@ -605,11 +636,9 @@ int select_coop_impl(const void *keys, long long size, const int *size_dev, int 
   a.hist = reinterpret_cast<unsigned *>(s.coop_hist);
   a.tiles = reinterpret_cast<unsigned *>(s.tiles);
   a.max_tiles = s.max_tiles;
-  const long long items = tiles * batch;
-  const int grid = (int)(items < maxg ? items : maxg);
   void *args[] = {&a};
-  GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K>, dim3(grid), dim3(SEL_THREADS),
-                                      args, 0, st));
+  GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K>, dim3((unsigned)(cpr * batch)),
+                                      dim3(CT), args, 0, st));
   GS_LAUNCHED();
   return GSFFT_OK;
 }
