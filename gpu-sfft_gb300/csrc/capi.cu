@@ -316,7 +316,7 @@ int gsfft_stage_reverse_hash(const int *d_J, int B_thresh, const int *d_J2, int 
   if (s == GSFFT_OK) s = launch_sigma_bitmaps(d_J2, ctl, num_RLFC, W_RLFC, 1, d, bm, ctl, st);
   if (s == GSFFT_OK)
     s = launch_vote_loop(0, d_J, B_thresh, n, B, W_RLFC, bm, d, loops_thresh, epoch, d_vote, d_cand,
-                         cap, cnt, blk, ctl, st);
+                         cap, cnt, blk, ctl, true, st);
   if (s == GSFFT_OK && cudaMemcpyAsync(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost, st) != cudaSuccess)
     s = GSFFT_ERR_CUDA;
   if (s == GSFFT_OK) s = sync_check(st, "gsfft_stage_reverse_hash");

@@ -265,10 +265,10 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
                       p.B_thresh, nullptr, P->selW, st, rmax_w, P->floor_rel));
   END(ST_RLFC_SELECT);
   BEGIN(ST_J2);
-  GS_CHECK(launch_j2_merge(P->J2b, p.RLFC_loops * p.B_thresh, p.W_RLFC, P->bm_j2, P->J2, P->ctl,
-                           P->tile_tmp, st));
-  GS_CHECK(launch_sigma_bitmaps(P->J2, P->ctl, p.RLFC_loops * p.B_thresh, p.W_RLFC, p.loops_loc, d,
-                                P->bm_sig, P->ctl, st));
+  // F_l needs only the set of J2 ids, not the sorted list; the sorted J2
+  // (num_RLFC ids) is compacted on demand by plan_debug
+  GS_CHECK(launch_sigma_from_blocks(P->J2b, p.RLFC_loops * p.B_thresh, p.W_RLFC, p.loops_loc, d,
+                                    P->bm_sig, P->ctl, st));
   END(ST_J2);
 
   // A6: bucket FFT of every loop, cutoff of the location loops
@@ -297,7 +297,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   for (int l = 0; l < p.loops_loc; l++)
     GS_CHECK(launch_vote_loop(l, P->J + (size_t)l * p.B_thresh, p.B_thresh, p.n, p.B, p.W_RLFC,
                               P->bm_sig + wW * l, d, p.loops_thresh, P->epoch, P->vote, P->cand,
-                              P->cap, P->cnt, P->blk, P->ctl, st));
+                              P->cap, P->cnt, P->blk, P->ctl, l + 1 >= p.loops_thresh, st));
   END(ST_VOTE);
   // A8: estimation; A9: k largest
   BEGIN(ST_ESTIMATE);
@@ -376,6 +376,9 @@ int plan_stage_times(Plan *P, float *ms_avg, int max_stages, int *runs) {
 int plan_debug(Plan *P, int *h_J2, int *num_RLFC, int *h_J, void *h_bins, cudaStream_t st) {
   if (!P->ran) return GSFFT_ERR_STATE;
   const gsfft_params &p = P->p;
+  if (h_J2 || num_RLFC)  // sorted, de-duplicated union of the last run's RLFC blocks
+    GS_CHECK(launch_j2_merge(P->J2b, p.RLFC_loops * p.B_thresh, p.W_RLFC, P->bm_j2, P->J2, P->ctl,
+                             P->tile_tmp, st));
   GS_CUDA(cudaStreamSynchronize(st));
   RunCtl c;
   GS_CUDA(cudaMemcpy(&c, P->ctl, sizeof(RunCtl), cudaMemcpyDeviceToHost));

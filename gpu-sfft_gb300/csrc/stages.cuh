@@ -51,19 +51,24 @@ int launch_perm_filter_stream(int precision, const void *x, int n, const void *f
 // J2 = sorted distinct union of the RLFC blocks, through a W-bit bitmap.
 int launch_j2_merge(const int *J2_blocks, int total, int W, unsigned *bitmap, int *J2,
                     RunCtl *ctl, unsigned *tile_tmp, cudaStream_t st);
-int j2_merge_launches();
 
 // Permuted-residue bitmaps F_l = {J2[m] * ai_l mod W} for the location loops,
 // and fmax_l = max F_l.
 int launch_sigma_bitmaps(const int *J2, const RunCtl *ctl_num, int max_num, int W, int loops_loc,
                          const Draws &d, unsigned *bitmaps, RunCtl *ctl, cudaStream_t st);
 
+// The same bitmaps and fmax_l straight from the RLFC blocks (total ids, with
+// duplicates); ctl->fmax must be zero on entry.
+int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, const Draws &d,
+                             unsigned *bitmaps, RunCtl *ctl, cudaStream_t st);
+
 // A7: one location loop of voting; appends candidates in canonical order.
+// may_complete = false (location loop l < loops_thresh - 1 of a run, where no
+// count can reach the threshold) only records the votes.
 int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
                      const unsigned *bitmap_l, const Draws &d, int loops_thresh, unsigned epoch,
                      unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
-                     cudaStream_t st);
-int vote_launches_per_loop();
+                     bool may_complete, cudaStream_t st);
 // ints needed by the blk scratch of launch_vote_loop
 int vote_block_ints(int B_thresh);
 

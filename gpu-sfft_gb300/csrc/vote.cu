@@ -129,6 +129,25 @@ __global__ void sigma_bits_kernel(const int *__restrict__ J2, const int *num_dev
   atomicMax(&fmax[l], (int)f);
 }
 
+// Same bitmaps straight from the RLFC blocks (duplicates set the same bit
+// twice), with the per-loop maximum reduced per warp before one atomic.
+__global__ void sigma_from_blocks_kernel(const int *__restrict__ J2b, int total, int W, Draws d,
+                                         int loops_loc, unsigned *bms, int words_per_map,
+                                         int *fmax) {
+  const int m = blockIdx.x * VT + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool ok = m < total;
+  const unsigned v = ok ? (unsigned)J2b[m] : 0u;
+  for (int l = 0; l < loops_loc; l++) {
+    const unsigned f = (v * (unsigned)d.ai[l]) & (unsigned)(W - 1);
+    if (ok) atomicOr(&bms[(size_t)l * words_per_map + (f >> 5)], 1u << (f & 31));
+    int mx = ok ? (int)f : -1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0 && mx >= 0) atomicMax(&fmax[l], mx);
+  }
+}
+
 // ------------------------------------------------------------ voting
 struct WalkArgs {
   const int *J;
@@ -219,14 +238,31 @@ vote_count_kernel(WalkArgs w, unsigned epoch, unsigned thresh, unsigned *vote, i
   if (t < w.Bt) {
     const unsigned nmask = (unsigned)w.n - 1u;
     for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
+      // up to four visited positions at a time: their table reads are
+      // independent, so they overlap instead of paying one DRAM latency each
       while (mask) {
-        const int b = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const unsigned loc = ((unsigned)pos(b) * w.a) & nmask;
-        const unsigned e = vote[loc];
-        const unsigned cv = ((e >> 8) == epoch) ? (e & 255u) + 1u : 1u;
-        vote[loc] = (epoch << 8) | cv;
-        c += (cv == thresh);
+        unsigned loc[4], e[4];
+        int nq = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (mask) {
+            const int b = __ffs(mask) - 1;
+            mask &= mask - 1;
+            loc[q] = ((unsigned)pos(b) * w.a) & nmask;
+            nq = q + 1;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (q < nq) e[q] = vote[loc[q]];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (q < nq) {
+            const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
+            vote[loc[q]] = (epoch << 8) | cv;
+            c += (cv == thresh);
+          }
+        }
       }
     });
   }
@@ -260,6 +296,40 @@ vote_count_kernel(WalkArgs w, unsigned epoch, unsigned thresh, unsigned *vote, i
   }
 }
 
+// Location loops before the (loops_thresh-1)-th cannot bring any count to
+// the threshold: they only record their votes.
+__global__ void __launch_bounds__(VT)
+vote_mark_kernel(WalkArgs w, unsigned epoch, unsigned *vote) {
+  const int warp = threadIdx.x >> 5;
+  const int t = blockIdx.x * WPB + warp;
+  if (t >= w.Bt) return;
+  const unsigned nmask = (unsigned)w.n - 1u;
+  for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
+    while (mask) {
+      unsigned loc[4], e[4];
+      int nq = 0;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (mask) {
+          const int b = __ffs(mask) - 1;
+          mask &= mask - 1;
+          loc[q] = ((unsigned)pos(b) * w.a) & nmask;
+          nq = q + 1;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (q < nq) e[q] = vote[loc[q]];
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (q < nq) {
+          const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
+          vote[loc[q]] = (epoch << 8) | cv;
+        }
+    }
+  });
+}
+
 __global__ void __launch_bounds__(VT)
 vote_write_kernel(WalkArgs w, unsigned epoch, unsigned thresh, const unsigned *__restrict__ vote,
                   const int *__restrict__ cnt, const int *__restrict__ blk_pre, int nblk, int *cand,
@@ -282,10 +352,20 @@ vote_write_kernel(WalkArgs w, unsigned epoch, unsigned thresh, const unsigned *_
       unsigned app = 0;
       unsigned m = mask;
       while (m) {
-        const int b = __ffs(m) - 1;
-        m &= m - 1;
-        const unsigned loc = ((unsigned)pos(b) * w.a) & nmask;
-        if (vote[loc] == want) app |= 1u << b;
+        unsigned loc[4], bit[4];
+        int nq = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (m) {
+            bit[q] = __ffs(m) - 1;
+            m &= m - 1;
+            loc[q] = ((unsigned)pos((int)bit[q]) * w.a) & nmask;
+            nq = q + 1;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (q < nq && vote[loc[q]] == want) app |= 1u << bit[q];
       }
       unsigned ctot;
       long long o = next + warp_excl_scan((unsigned)__popc(app), &ctot);
@@ -316,8 +396,6 @@ vote_write_kernel(WalkArgs w, unsigned epoch, unsigned thresh, const unsigned *_
 
 }  // namespace
 
-int j2_merge_launches() { return 3; }
-
 int launch_j2_merge(const int *J2_blocks, int total, int W, unsigned *bitmap, int *J2, RunCtl *ctl,
                     unsigned *tile_tmp, cudaStream_t st) {
   const int nwords = W / 32;
@@ -343,12 +421,21 @@ int launch_sigma_bitmaps(const int *J2, const RunCtl *ctl_num, int max_num, int 
   return GSFFT_OK;
 }
 
-int vote_launches_per_loop() { return 2; }
+int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, const Draws &d,
+                             unsigned *bitmaps, RunCtl *ctl, cudaStream_t st) {
+  const int words = W / 32;
+  GS_CUDA(cudaMemsetAsync(bitmaps, 0, sizeof(unsigned) * (size_t)words * loops_loc, st));
+  // ctl->fmax starts at 0 (the run clears RunCtl); every F_l is non-empty
+  sigma_from_blocks_kernel<<<(total + VT - 1) / VT, VT, 0, st>>>(J2b, total, W, d, loops_loc,
+                                                                  bitmaps, words, ctl->fmax);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
 
 int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
                      const unsigned *bitmap_l, const Draws &d, int loops_thresh, unsigned epoch,
                      unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
-                     cudaStream_t st) {
+                     bool may_complete, cudaStream_t st) {
   WalkArgs w;
   w.J = J;
   w.Bt = B_thresh;
@@ -359,6 +446,11 @@ int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
   w.fmax = &ctl->fmax[l];
   w.a = (unsigned)d.a[l];
   const int grid = (B_thresh + WPB - 1) / WPB;
+  if (!may_complete) {
+    vote_mark_kernel<<<grid, VT, 0, st>>>(w, epoch, vote);
+    GS_LAUNCHED();
+    return GSFFT_OK;
+  }
   int *blk_pre = blk + grid + 1;  // blk holds 2 * (grid + 1) ints
   vote_count_kernel<<<grid, VT, 0, st>>>(w, epoch, (unsigned)loops_thresh, vote, cnt, blk, blk_pre,
                                          ctl);
