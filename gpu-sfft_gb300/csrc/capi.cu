@@ -252,22 +252,26 @@ int gsfft_stage_perm_filter_stream(int precision, const void *d_x, int n,
   memset(&d, 0, sizeof(d));
   for (int l = 0; l < loops; l++) d.a[l] = h_a[l];
   const bool fl = precision == GSFFT_MIXED;
-  void *taps = nullptr, *part = nullptr;
+  void *taps = nullptr, *part = nullptr, *tbm = nullptr;
   int *err = nullptr;
   const int groups = stream_pf_groups(n, B, loops, precision);
   const size_t es = fl ? sizeof(float2) : sizeof(double2);
   if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return GSFFT_ERR_ALLOC;
   if (cudaMalloc(&part, es * (size_t)groups * loops * B) != cudaSuccess ||
+      cudaMalloc(&tbm, es * (size_t)stream_taps_count(w, B)) != cudaSuccess ||
       (fl && cudaMalloc(&taps, sizeof(float2) * (size_t)w) != cudaSuccess)) {
     cudaFree(err);
     if (part) cudaFree(part);
+    if (tbm) cudaFree(tbm);
     return GSFFT_ERR_ALLOC;
   }
   int s = cudaMemsetAsync(err, 0, sizeof(int), S(stream)) == cudaSuccess ? GSFFT_OK : GSFFT_ERR_CUDA;
   if (s == GSFFT_OK && fl) s = launch_convert_taps((const double2 *)d_filter_time, taps, w, true, S(stream));
   if (s == GSFFT_OK)
-    s = launch_perm_filter_stream(precision, d_x, n, fl ? taps : (const void *)d_filter_time, w, B,
-                                  loops, d, part, 0, nullptr, n, err, S(stream));
+    s = launch_stream_taps(precision, fl ? taps : (const void *)d_filter_time, w, B, tbm, S(stream));
+  if (s == GSFFT_OK)
+    s = launch_perm_filter_stream(precision, d_x, n, tbm, w, B, loops, d, part, 0, nullptr, n, err,
+                                  S(stream));
   if (s == GSFFT_OK)
     s = launch_sum_partials(precision, part, groups, (long long)loops * B, d_bins, S(stream));
   if (s == GSFFT_OK) s = sync_check(S(stream), "gsfft_stage_perm_filter_stream");
@@ -279,6 +283,7 @@ int gsfft_stage_perm_filter_stream(int precision, const void *d_x, int n,
     s = GSFFT_ERR_CUDA;
   }
   if (taps) cudaFree(taps);
+  cudaFree(tbm);
   cudaFree(part);
   cudaFree(err);
   return s;

@@ -4,6 +4,7 @@
 // Data layout in HBM (T = double in FP64 mode, float in MIXED mode):
 //   x            n complex T (caller)             signal
 //   filt         w complex T                      filter taps
+//   filt_bm      B x (w/B + 1) complex T          the taps bucket-major (streaming form)
 //   hinv         n/B + 1 complex double           conj(H)/|H|^2 around bin 0
 //   rsamp        RLFC_loops x W_RLFC T            |FFT_W(restricted x)|^2
 //   J2b / J2     RLFC_loops x B_thresh int        RLFC blocks / merged ids
@@ -122,6 +123,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
     P->groups = stream_pf_groups(p.n, p.B, p.loops, precision);
     A(ybuf, V * (size_t)p.RLFC_loops * p.W_RLFC);
     A(bpart, V * (size_t)P->groups * p.loops * p.B);
+    A(filt_bm, V * (size_t)stream_taps_count(p.w, p.B));
   }
 #undef A
   P->floor_rel = (flags & GSFFT_FLAG_RAW_SELECTION) ? 0.0 : 1e-10;
@@ -152,7 +154,8 @@ void plan_destroy(Plan *P) {
   if (!P) return;
   void *ptrs[] = {P->filt, P->hinv, P->rsamp, P->J2b, P->J2, P->bins, P->bsamp, P->J,
                   P->bm_j2, P->bm_sig, P->tile_tmp, P->vote, P->cand, P->cnt, P->blk,
-                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax, P->ybuf, P->bpart};
+                  P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax, P->ybuf, P->bpart,
+                  P->filt_bm};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
@@ -180,6 +183,7 @@ int plan_set_filter(Plan *P, const void *d_ft, const void *d_ff, cudaStream_t st
   const gsfft_params &p = P->p;
   if (!d_ft || !d_ff) return GSFFT_ERR_PARAM;
   GS_CHECK(launch_convert_taps((const double2 *)d_ft, P->filt, p.w, P->precision == GSFFT_MIXED, st));
+  if (P->use_stream) GS_CHECK(launch_stream_taps(P->precision, P->filt, p.w, p.B, P->filt_bm, st));
   GS_CHECK(launch_hinv((const double2 *)d_ff, p.n, p.n / p.B, P->hinv, st));
   GS_CUDA(cudaStreamSynchronize(st));
   P->filter_set = true;
@@ -235,7 +239,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   // A5 (+ RLFC sub-sampling when streaming): bins of every loop
   BEGIN(ST_PERM_FILTER);
   if (P->use_stream)
-    GS_CHECK(launch_perm_filter_stream(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d,
+    GS_CHECK(launch_perm_filter_stream(P->precision, d_x, p.n, P->filt_bm, p.w, p.B, p.loops, d,
                                        P->bpart, p.RLFC_loops, P->ybuf, p.W_RLFC, &P->ctl->err, st));
   else
     GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d, quirk,

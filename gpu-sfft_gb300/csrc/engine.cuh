@@ -40,6 +40,7 @@ struct Plan {
   void *rmax = nullptr;  // per-row maxima: RLFC_loops rows then loops rows (u64 each)
   void *ybuf = nullptr;  // RLFC sub-samples written by the streaming perm+filter
   void *bpart = nullptr; // row-group partial bins of the streaming perm+filter
+  void *filt_bm = nullptr; // bucket-major taps of the streaming perm+filter
   int groups = 1;
   bool use_stream = false;
   double floor_rel = 1e-10;

@@ -155,6 +155,7 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   const int nb = 1 << lognb;
   const unsigned nbm = (unsigned)nb - 1u;
   const unsigned nmask = (1u << logn) - 1u;
+  const int TT = tiles + 1;  // taps per bucket in the bucket-major table
   const unsigned stage_bytes = (unsigned)(rt * CW * sizeof(V));
   const int ntile = rows_per_group / rt;
   const int ncb = B / CW;
@@ -252,14 +253,14 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     }
     int mc = mw + lo;
     const int me = mw + tiles;
-    const V *fcol = filt + bl;
+    const V *fcol = filt + (size_t)bl * TT;  // the bucket's taps, contiguous
     unsigned nm = NONE, er = NONE;
     // taps of the next PFD hits, loaded ahead (the last entries of the
     // doubled list are valid indices, so loading past me is harmless)
     V fv[PFD];
 #pragma unroll
     for (int u = 0; u < PFD; u++)
-      fv[u] = ld_tap(fcol + ((size_t)(S[min(mc + u, 2 * tiles - 1)] & 255u) << logB), keep);
+      fv[u] = ld_tap(fcol + (S[min(mc + u, 2 * tiles - 1)] & 255u), keep);
     V fe = mk((T)0, (T)0);
     if (mc < me) {
       const unsigned ent = S[mc];
@@ -268,7 +269,7 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     if (bl < residue) {
       er = (xrow + sl) & nbm;
       if (er < (unsigned)rbeg) er = NONE;
-      else fe = ld_tap(fcol + ((size_t)tiles << logB), keep);
+      else fe = ld_tap(fcol + tiles, keep);
     }
     T re = 0, im = 0;
 
@@ -292,7 +293,7 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
 #pragma unroll
         for (int u = 0; u + 1 < PFD; u++) fv[u] = fv[u + 1];
         const int m = ++mc;
-        fv[PFD - 1] = ld_tap(fcol + ((size_t)(S[min(m + PFD - 1, 2 * tiles - 1)] & 255u) << logB), keep);
+        fv[PFD - 1] = ld_tap(fcol + (S[min(m + PFD - 1, 2 * tiles - 1)] & 255u), keep);
         nm = m < me ? (S[m] >> 8) + sl - (m < tiles ? (unsigned)nb : 0u) : NONE;
       }
       if (er < r1) {
@@ -323,6 +324,18 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     // partial sums of this row group: bins[group][l][b]
     bins[((size_t)g * L + l) * B + bl] = mk(re, im);
   }
+}
+
+// Bucket-major copy of the taps: tb[b * TT + j] = filt[j * B + b] (0 past w).
+template <typename V>
+__global__ void bucket_major_kernel(const V *__restrict__ filt, int w, int B, int TT, V *tb) {
+  const long long i = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (i >= (long long)B * TT) return;
+  const int b = (int)(i / TT), j = (int)(i % TT);
+  const long long src = (long long)j * B + b;
+  V v = filt[src < w ? src : 0];
+  if (src >= w) v.x = v.y = 0;
+  tb[i] = v;
 }
 
 template <typename V>
@@ -406,6 +419,21 @@ int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int l
 }
 
 }  // namespace
+
+int stream_taps_count(int w, int B) { return B * (w / B + 1); }
+
+int launch_stream_taps(int precision, const void *filt, int w, int B, void *taps_bm,
+                       cudaStream_t st) {
+  const int TT = w / B + 1;
+  const long long cnt = (long long)B * TT;
+  const unsigned grid = (unsigned)((cnt + 255) / 256);
+  if (precision == GSFFT_FP64)
+    bucket_major_kernel<double2><<<grid, 256, 0, st>>>((const double2 *)filt, w, B, TT, (double2 *)taps_bm);
+  else
+    bucket_major_kernel<float2><<<grid, 256, 0, st>>>((const float2 *)filt, w, B, TT, (float2 *)taps_bm);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
 
 int launch_sum_partials(int precision, const void *part, int groups, long long count, void *out,
                         cudaStream_t st) {
