@@ -48,7 +48,7 @@ constexpr int CTAS_PER_SM = 2;
 constexpr unsigned NONE = 0x7fffffffu;
 
 // columns per work item: one consumer thread per (column, loop)
-inline int cols_per_item(int loops) { return 64 * loops + 32 <= 1024 ? 64 : 32; }
+inline int cols_per_item(int loops) { return 64 * loops + 64 <= 1024 ? 64 : 32; }
 
 struct HitTab {
   unsigned s[MAXL][MAXT];  // (row offset << 8) | j, sorted by row offset
@@ -126,13 +126,17 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 }
 
 // Persistent, warp-specialised.  A work item is (block of CW columns, row
-// group); CTA b takes items b, b + grid, ...  The last warp is the producer:
-// one lane streams every tile of the CTA's items, in order, into an NSTAGE
-// ring (full[s]: tile landed, tx-counted; empty[s]: every consumer warp is
-// done with it).  The other CW * loops threads are consumers: thread (l, col)
-// walks loop l of column col, so each warp covers 32 columns of one loop; the
-// tap of its next hit is loaded one hit ahead so the scattered L2 reads
-// overlap the stream.  No block-wide barrier inside the stream.
+// group); CTA b takes items b, b + grid, ...  Warp roles:
+//  * threads [0, CW*loops): consumers.  Thread (l, col) walks loop l of
+//    column col, so each warp covers 32 columns of one loop; the tap of its
+//    next hit is loaded one hit ahead (from the bucket-major tap table) so
+//    the L2 reads overlap the stream.
+//  * the next warp: producer.  One lane streams every tile of the CTA's
+//    items, in order, into an NSTAGE ring (full[s]: tile landed, tx-counted;
+//    empty[s]: every releasing warp is done with it).
+//  * the last warp (RLFC loops only): copies the RLFC sub-samples out of
+//    each tile.
+// No block-wide barrier inside the stream.
 template <typename T, int CW, int MAXTH>
 __global__ void __launch_bounds__(MAXTH, MAXTH <= 640 ? CTAS_PER_SM : 1)
 pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V *__restrict__ filt,
@@ -143,6 +147,7 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   constexpr int LOGCW = CW == 64 ? 6 : 5;
   const int NCT = CW * L;  // consumer threads
   const int NCW = NCT / 32;
+  const int NREL = NCW + (nrlfc > 0 ? 1 : 0);  // warps releasing each stage
   extern __shared__ __align__(128) unsigned char dsm[];
   // each loop's sorted list twice in a row, so a rotated walk needs no wrap
   __shared__ unsigned S2[MAXL][2 * MAXT];
@@ -176,12 +181,50 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     abort_flag = 0;
     for (int s = 0; s < NSTAGE; s++) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], NCW);
+      mbar_init(&empty[s], NREL);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
 
+  const unsigned smask = (1u << logsig) - 1u;
+  if (tid >= NCT + 32) {
+    // ---------------- RLFC warp: loop r samples positions off_r + m*(n/W)
+    // (restLocFreqCoeffKernel, innerLoop.cu:693-703); n/W divides B, so those
+    // are whole columns, copied from the tile to y_r[t / (n/W)]
+    if (nrlfc == 0) return;
+    const int lane = tid & 31;
+    long long k = 0;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+      const int cb = it % ncb, g = it / ncb;
+      const int c0 = cb * CW;
+      for (int t = 0; t < ntile; t++, k++) {
+        const int st = (int)(k % NSTAGE);
+        const V *tl = tile0 + (size_t)st * rt * CW;
+        if (!mbar_wait(&full[st], (unsigned)((k / NSTAGE) & 1))) {
+          abort_flag = 1;
+          atomicExch(err, 1);
+          return;
+        }
+        const unsigned r0 = (unsigned)(g * rows_per_group + t * rt);
+        for (int rr = 0; rr < nrlfc; rr++) {
+          const unsigned off = (unsigned)d.offs[rr];
+          const unsigned first = ((off - (unsigned)c0) & smask);  // first matching column
+          if (first >= (unsigned)CW) continue;
+          const int lognc = logsig >= LOGCW ? 0 : LOGCW - logsig;  // log2 of the column count
+          for (int e = lane; e < (rt << lognc); e += 32) {
+            const int row = e >> lognc, ci = e & ((1 << lognc) - 1);
+            const unsigned cc = first + ((unsigned)ci << logsig);
+            const unsigned tpos = ((r0 + row) << logB) + (unsigned)c0 + cc;
+            y[(size_t)rr * W + ((tpos - off) >> logsig)] = tl[(row << LOGCW) + cc];
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+      }
+    }
+    return;
+  }
   if (tid >= NCT) {
     // ---------------- producer
     if (tid == NCT) {
@@ -215,7 +258,6 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   // ---------------- consumers
   const int col = tid & (CW - 1), l = tid >> LOGCW, lane = tid & 31;
   const int residue = w & (B - 1);
-  const unsigned smask = (1u << logsig) - 1u;
   const unsigned a = s_a[l], beta = s_beta[l], xrow = s_xrow[l];
   const unsigned *S = S2[l];
   const unsigned long long keep = policy_evict_last();
@@ -304,20 +346,6 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
         im = fma(xv.y, fe.x, im);
         er = NONE;
       }
-      // RLFC sub-samples held by this tile: columns c == off (mod n/W); with
-      // n/W <= CW there are CW >> logsig of them, else at most one
-      for (int rr = 0; rr < nrlfc; rr++) {
-        const unsigned off = (unsigned)d.offs[rr];
-        const unsigned first = ((off - (unsigned)c0) & smask);  // first matching column index
-        if (first >= (unsigned)CW) continue;
-        const int lognc = logsig >= LOGCW ? 0 : LOGCW - logsig;  // log2 of the column count
-        for (int e = tid; e < (rt << lognc); e += NCT) {
-          const int row = e >> lognc, ci = e & ((1 << lognc) - 1);
-          const unsigned cc = first + ((unsigned)ci << logsig);
-          const unsigned tpos = ((r0 + row) << logB) + (unsigned)c0 + cc;
-          y[(size_t)rr * W + ((tpos - off) >> logsig)] = tl[(row << LOGCW) + cc];
-        }
-      }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[st]);
     }
@@ -379,7 +407,7 @@ int launch_CW(const CUtensorMap &tm, const void *filt, int logn, int logB, int w
   typedef typename Cx<T>::V V;
   const int B = 1 << logB;
   const int smem = NSTAGE * rt * CW * (int)sizeof(V);
-  const int threads = CW * loops + 32;
+  const int threads = CW * loops + (nrlfc > 0 ? 64 : 32);
   static int attr = 0;
   if (attr < smem) {
     GS_CUDA(cudaFuncSetAttribute(pf_tma_kernel<T, CW, MAXTH>,
@@ -405,7 +433,7 @@ int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int l
              int tiles, int groups, const Draws &d, const HitTab &ht, void *bins, int nrlfc,
              int logsig, void *y, int W, int *err, cudaStream_t st) {
   const int cw = cols_per_item(loops);
-  const bool small = cw * loops + 32 <= 640;
+  const bool small = cw * loops + (nrlfc > 0 ? 64 : 32) <= 640;
 #define GO(CWV, MT)                                                                                \
   return launch_CW<T, CWV, MT>(tm, filt, logn, logB, w, rt, tiles, groups, loops, d, ht, bins, nrlfc, \
                                logsig, y, W, err, st)
