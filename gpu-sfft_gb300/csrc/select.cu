@@ -364,6 +364,9 @@ constexpr int MAXB = 8;         // rows per cooperative call
 constexpr int CT = 512;         // threads per CTA
 constexpr int SPT = 8;          // contiguous samples per thread in the write pass
 constexpr int CHUNK_MIN = 8192; // smallest chunk per CTA
+constexpr int UN = 8;           // loads in flight per thread in the scan passes
+constexpr int COOP_SMEM = (CT / 32) * (HIST_BINS / 2) * 4;  // per-warp histograms
+constexpr long long MAX_CHUNK = 16LL * 65535;  // keeps a warp's 16-bit counters exact
 
 struct CoopArgs {
   const void *keys;
@@ -412,7 +415,9 @@ __device__ __forceinline__ unsigned ct_excl_scan(unsigned v, unsigned *ws, unsig
 template <typename K>
 __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
   cg::grid_group grid = cg::this_grid();
-  __shared__ unsigned sh[HIST_BINS];
+  // one private histogram per warp, two 16-bit counters per word, so warps
+  // never contend on a bin (a warp counts at most chunk / 16 < 65536 keys)
+  extern __shared__ unsigned wh[];  // [CT / 32][HIST_BINS / 2]
   __shared__ unsigned ws[CT / 32];
   __shared__ unsigned long long s_prefix;
   __shared__ long long s_rank;
@@ -457,25 +462,48 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
       const unsigned dmask = (1u << width) - 1u;
       const unsigned long long hi_mask =
           (shift + width >= kb) ? 0ull : (~0ull << (shift + width)) & (kb == 64 ? ~0ull : 0xffffffffull);
-      for (int i = tid; i < HIST_BINS; i += CT) sh[i] = 0;
-      __syncthreads();
-      for (long long base = lo; base < hi; base += CT) {
-        const long long i = base + tid;
-        bool hit = false;
-        unsigned digit = 0;
-        if (i < hi) {
-          const unsigned long long k = (unsigned long long)load_key<K>(row, i, floor);
-          hit = (k & hi_mask) == prefix;
-          digit = (unsigned)(k >> shift) & dmask;
+      unsigned *mine = wh + (tid >> 5) * (HIST_BINS / 2);
+      for (int i = lane; i < HIST_BINS / 2; i += 32) mine[i] = 0;
+      __syncwarp();
+      // UN independent loads per thread in flight before the histogram updates
+      for (long long base = lo; base < hi; base += (long long)CT * UN) {
+        unsigned long long kv[UN];
+#pragma unroll
+        for (int u = 0; u < UN; u++) {
+          const long long i = base + (long long)u * CT + tid;
+          kv[u] = i < hi ? (unsigned long long)load_key<K>(row, i, floor) : ~0ull;
         }
-        const unsigned key = hit ? digit : (0x80000000u | (unsigned)lane);
-        const unsigned peers = __match_any_sync(0xffffffffu, key);
-        if (hit && lane == __ffs(peers) - 1) atomicAdd(&sh[digit], (unsigned)__popc(peers));
+#pragma unroll
+        for (int u = 0; u < UN; u++) {
+          const long long i = base + (long long)u * CT + tid;
+          const bool hit = i < hi && (kv[u] & hi_mask) == prefix;
+          const unsigned digit = (unsigned)(kv[u] >> shift) & dmask;
+          // a warp whose keys share one digit (floored zeros, a dense peak)
+          // adds once; otherwise every lane adds its own key (the private
+          // per-warp table only sees same-word collisions inside the warp)
+          const unsigned d0 = __shfl_sync(0xffffffffu, digit, 0);
+          const unsigned hits = __ballot_sync(0xffffffffu, hit);
+          if (hits == 0xffffffffu && __all_sync(0xffffffffu, digit == d0)) {
+            if (lane == 0) atomicAdd(&mine[d0 >> 1], 32u << ((d0 & 1u) * 16));
+          } else if (hit) {
+            atomicAdd(&mine[digit >> 1], 1u << ((digit & 1u) * 16));
+          }
+        }
       }
       __syncthreads();
       unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
-      for (int i = tid; i < HIST_BINS; i += CT)
-        if (sh[i]) atomicAdd(&gh[i], sh[i]);
+      for (int word = tid; word < HIST_BINS / 2; word += CT) {
+        unsigned lo16 = 0, hi16 = 0;
+#pragma unroll 4
+        for (int wv = 0; wv < CT / 32; wv++) {
+          const unsigned v = wh[wv * (HIST_BINS / 2) + word];
+          lo16 += v & 0xffffu;
+          hi16 += v >> 16;
+        }
+        if (lo16) atomicAdd(&gh[2 * word], lo16);
+        if (hi16) atomicAdd(&gh[2 * word + 1], hi16);
+      }
+      __syncthreads();  // the per-warp histograms are rebuilt next pass
     }
     grid.sync();
     if (!done) {
@@ -521,10 +549,20 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
   const unsigned long long thr_c = (unsigned long long)thr >> cmp_shift;
   unsigned gt = 0, eq = 0;
   if (!take_all) {
-    for (long long i = lo + tid; i < hi; i += CT) {
-      const unsigned long long kc = (unsigned long long)load_key<K>(row, i, floor) >> cmp_shift;
-      gt += kc > thr_c;
-      eq += kc == thr_c;
+    for (long long base = lo; base < hi; base += (long long)CT * UN) {
+      unsigned long long kv[UN];
+#pragma unroll
+      for (int u = 0; u < UN; u++) {
+        const long long i = base + (long long)u * CT + tid;
+        kv[u] = i < hi ? (unsigned long long)load_key<K>(row, i, floor) : 0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < UN; u++) {
+        const long long i = base + (long long)u * CT + tid;
+        const unsigned long long kc = kv[u] >> cmp_shift;
+        gt += i < hi && kc > thr_c;
+        eq += i < hi && kc == thr_c;
+      }
     }
   }
   unsigned tgt, teq;
@@ -604,7 +642,10 @@ int coop_grid() {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (!coop) return -1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K>, CT, 0);
+    if (cudaFuncSetAttribute(sel_coop_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             COOP_SMEM) != cudaSuccess)
+      return -1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K>, CT, COOP_SMEM);
     g = per > 0 ? per * sms : -1;
   }
   return g;
@@ -619,7 +660,7 @@ int select_coop_impl(const void *keys, long long size, const int *size_dev, int 
   long long cpr = (size + CHUNK_MIN - 1) / CHUNK_MIN;
   if (cpr > maxg / batch) cpr = maxg / batch;
   if (cpr > s.max_tiles) cpr = s.max_tiles;
-  if (cpr < 1) return GSFFT_ERR_UNSUPPORTED;
+  if (cpr < 1 || (size + cpr - 1) / cpr + 32 > MAX_CHUNK) return GSFFT_ERR_UNSUPPORTED;
   CoopArgs a;
   a.keys = keys;
   a.size = size;
@@ -638,7 +679,7 @@ int select_coop_impl(const void *keys, long long size, const int *size_dev, int 
   a.max_tiles = s.max_tiles;
   void *args[] = {&a};
   GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K>, dim3((unsigned)(cpr * batch)),
-                                      dim3(CT), args, 0, st));
+                                      dim3(CT), args, COOP_SMEM, st));
   GS_LAUNCHED();
   return GSFFT_OK;
 }
