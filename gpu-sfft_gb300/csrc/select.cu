@@ -363,7 +363,7 @@ namespace cg = cooperative_groups;
 constexpr int MAXB = 8;         // rows per cooperative call
 constexpr int CT = 512;         // threads per CTA
 constexpr int SPT = 8;          // contiguous samples per thread in the write pass
-constexpr int CHUNK_MIN = 8192; // smallest chunk per CTA
+constexpr int CHUNK_MIN = 2048; // smallest chunk per CTA
 constexpr int UN = 8;           // loads in flight per thread in the scan passes
 constexpr int COOP_SMEM = (CT / 32) * (HIST_BINS / 2) * 4;  // per-warp histograms
 constexpr long long MAX_CHUNK = 16LL * 65535;  // keeps a warp's 16-bit counters exact
@@ -381,6 +381,7 @@ struct CoopArgs {
   double floor_rel;
   unsigned *hist;        // [6][MAXB][HIST_BINS], zero on entry and on exit
   unsigned *tiles;       // [MAXB][max_tiles][2]: per-chunk (#greater, #equal)
+  unsigned *zero_count;  // [MAXB] zeros per row, zero on entry and on exit
   int max_tiles;
 };
 
@@ -454,6 +455,46 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
   long long rank = sz - a.num - 1;
   int cmp_shift = 0;  // low bits ignored by the final comparisons
   bool done = take_all;
+  bool counted = false;  // the chunk counts for the final threshold are already stored
+  // (grid-uniform condition: every CTA reaches the same grid syncs)
+  if (a.row_max && a.floor_rel > 0.0) {
+    const bool mine_row = !take_all && floor != 0;
+    // With a rounding floor most samples of a noiseless spectrum read as 0.
+    // Count this chunk's zeros first: when the threshold's rank falls among
+    // the row's zeros the threshold is 0 and the per-chunk (nonzero, zero)
+    // counts are exactly the (#greater, #equal) counts the write pass needs.
+    unsigned nz = 0, zc = 0;
+    for (long long base = lo; mine_row && base < hi; base += (long long)CT * UN) {
+      K kv[UN];
+#pragma unroll
+      for (int u = 0; u < UN; u++) {
+        const long long i = base + (long long)u * CT + tid;
+        kv[u] = i < hi ? load_key<K>(row, i, floor) : (K)1;
+      }
+#pragma unroll
+      for (int u = 0; u < UN; u++) {
+        const long long i = base + (long long)u * CT + tid;
+        if (i < hi) {
+          nz += kv[u] != 0;
+          zc += kv[u] == 0;
+        }
+      }
+    }
+    unsigned tnz, tz;
+    ct_excl_scan(nz, ws, &tnz);
+    ct_excl_scan(zc, ws, &tz);
+    if (tid == 0 && mine_row) {
+      a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 0] = tnz;
+      a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = tz;
+      atomicAdd(&a.zero_count[b], tz);
+    }
+    grid.sync();
+    const long long zrow = (long long)__ldcg(&a.zero_count[b]);
+    if (mine_row && zrow > rank) {  // ascending rank `rank` is a zero
+      done = true;
+      counted = true;
+    }
+  }
   int shift = kb;
   for (int p = 0; p < npass; p++) {
     const int width = kb == 64 ? w64[p] : w32[p];
@@ -465,7 +506,11 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
       unsigned *mine = wh + (tid >> 5) * (HIST_BINS / 2);
       for (int i = lane; i < HIST_BINS / 2; i += 32) mine[i] = 0;
       __syncwarp();
-      // UN independent loads per thread in flight before the histogram updates
+      // UN independent loads per thread in flight before the histogram
+      // updates.  Digit 0 (floored zeros dominate the first pass of a
+      // noiseless spectrum) is counted in a register; other digits go to the
+      // warp's private table, where only collisions inside the warp remain.
+      unsigned zeros = 0;
       for (long long base = lo; base < hi; base += (long long)CT * UN) {
         unsigned long long kv[UN];
 #pragma unroll
@@ -476,20 +521,15 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
 #pragma unroll
         for (int u = 0; u < UN; u++) {
           const long long i = base + (long long)u * CT + tid;
-          const bool hit = i < hi && (kv[u] & hi_mask) == prefix;
-          const unsigned digit = (unsigned)(kv[u] >> shift) & dmask;
-          // a warp whose keys share one digit (floored zeros, a dense peak)
-          // adds once; otherwise every lane adds its own key (the private
-          // per-warp table only sees same-word collisions inside the warp)
-          const unsigned d0 = __shfl_sync(0xffffffffu, digit, 0);
-          const unsigned hits = __ballot_sync(0xffffffffu, hit);
-          if (hits == 0xffffffffu && __all_sync(0xffffffffu, digit == d0)) {
-            if (lane == 0) atomicAdd(&mine[d0 >> 1], 32u << ((d0 & 1u) * 16));
-          } else if (hit) {
-            atomicAdd(&mine[digit >> 1], 1u << ((digit & 1u) * 16));
+          if (i < hi && (kv[u] & hi_mask) == prefix) {
+            const unsigned digit = (unsigned)(kv[u] >> shift) & dmask;
+            if (digit == 0) zeros++;
+            else atomicAdd(&mine[digit >> 1], 1u << ((digit & 1u) * 16));
           }
         }
       }
+      zeros = __reduce_add_sync(0xffffffffu, zeros);
+      if (lane == 0 && zeros) atomicAdd(&mine[0], zeros);  // bin 0 = low half of word 0
       __syncthreads();
       unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
       for (int word = tid; word < HIST_BINS / 2; word += CT) {
@@ -548,7 +588,7 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
   const K thr = (K)prefix;
   const unsigned long long thr_c = (unsigned long long)thr >> cmp_shift;
   unsigned gt = 0, eq = 0;
-  if (!take_all) {
+  if (!take_all && !counted) {
     for (long long base = lo; base < hi; base += (long long)CT * UN) {
       unsigned long long kv[UN];
 #pragma unroll
@@ -568,11 +608,12 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
   unsigned tgt, teq;
   ct_excl_scan(gt, ws, &tgt);
   ct_excl_scan(eq, ws, &teq);
-  if (tid == 0) {
+  if (tid == 0 && !counted) {
     a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 0] = tgt;
     a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = teq;
   }
   grid.sync();
+  if (blockIdx.x == 0 && tid < MAXB) a.zero_count[tid] = 0;  // read by every CTA before the sync above
   // every CTA has read the histograms: zero them for the next call
   for (long long i = (long long)blockIdx.x * CT + tid; i < (long long)npass * MAXB * HIST_BINS;
        i += (long long)gridDim.x * CT)
@@ -601,30 +642,36 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
     unsigned gt_run = s_bg, eq_run = s_be;
     for (long long base = lo; base < hi; base += (long long)CT * SPT) {
       const long long i0 = base + (long long)tid * SPT;
-      unsigned flags = 0, ng = 0, ne = 0;  // bit 2q: greater, bit 2q+1: equal
+      unsigned gm = 0, em = 0;  // bit q: sample i0 + q is greater / equal
 #pragma unroll
       for (int q = 0; q < SPT; q++) {
         const long long i = i0 + q;
         if (i < hi) {
           const unsigned long long kc = (unsigned long long)load_key<K>(row, i, floor) >> cmp_shift;
-          const unsigned g = kc > thr_c, e = kc == thr_c;
-          flags |= (g << (2 * q)) | (e << (2 * q + 1));
-          ng += g;
-          ne += e;
+          gm |= (unsigned)(kc > thr_c) << q;
+          em |= (unsigned)(kc == thr_c) << q;
         }
       }
       unsigned tot;
-      const unsigned pre = ct_excl_scan(ng | (ne << 16), ws, &tot);
-      unsigned gb = gt_run + (pre & 0xffffu), eb = eq_run + (pre >> 16);
-#pragma unroll
-      for (int q = 0; q < SPT; q++) {
-        const unsigned g = (flags >> (2 * q)) & 1u, e = (flags >> (2 * q + 1)) & 1u;
-        if (g || (e && eb < need_eq)) {
-          const unsigned pos = gb + (eb < need_eq ? eb : need_eq);
-          if (pos < (unsigned)a.num) o[pos] = (int)(i0 + q);
+      const unsigned pre = ct_excl_scan((unsigned)__popc(gm) | ((unsigned)__popc(em) << 16), ws, &tot);
+      const unsigned gb = gt_run + (pre & 0xffffu), eb = eq_run + (pre >> 16);
+      // equal samples are taken while fewer than need_eq equal ones precede
+      unsigned take = gm;
+      if (eb < need_eq) {
+        unsigned room = need_eq - eb, m = em;
+        while (m && room) {
+          take |= m & (0u - m);
+          m &= m - 1;
+          room--;
         }
-        gb += g;
-        eb += e;
+      }
+      while (take) {
+        const int q = __ffs(take) - 1;
+        take &= take - 1;
+        const unsigned below = (1u << q) - 1u;
+        const unsigned eq_before = eb + (unsigned)__popc(em & below);
+        const unsigned pos = gb + (unsigned)__popc(gm & below) + (eq_before < need_eq ? eq_before : need_eq);
+        if (pos < (unsigned)a.num) o[pos] = (int)(i0 + q);
       }
       gt_run += tot & 0xffffu;
       eq_run += tot >> 16;
@@ -676,6 +723,7 @@ int select_coop_impl(const void *keys, long long size, const int *size_dev, int 
   a.floor_rel = floor_rel;
   a.hist = reinterpret_cast<unsigned *>(s.coop_hist);
   a.tiles = reinterpret_cast<unsigned *>(s.tiles);
+  a.zero_count = reinterpret_cast<unsigned *>(s.coop_hist) + 6 * MAXB * HIST_BINS;
   a.max_tiles = s.max_tiles;
   void *args[] = {&a};
   GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K>, dim3((unsigned)(cpr * batch)),
@@ -694,8 +742,8 @@ int select_scratch_init(SelectScratch &s, int max_batch, long long max_size) {
   GS_CUDA(cudaMalloc(&s.state, sizeof(SelState) * max_batch));
   GS_CUDA(cudaMalloc(&s.tiles, sizeof(unsigned) * 4 * (size_t)s.max_tiles * max_batch));
   GS_CUDA(cudaMemset(s.state, 0, sizeof(SelState) * max_batch));
-  GS_CUDA(cudaMalloc(&s.coop_hist, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
-  GS_CUDA(cudaMemset(s.coop_hist, 0, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
+  GS_CUDA(cudaMalloc(&s.coop_hist, sizeof(unsigned) * (6 * MAXB * HIST_BINS + MAXB)));
+  GS_CUDA(cudaMemset(s.coop_hist, 0, sizeof(unsigned) * (6 * MAXB * HIST_BINS + MAXB)));
   return GSFFT_OK;
 }
 
