@@ -55,6 +55,10 @@ def workload_config(cfg, extra=None):
     return d
 
 
+def workload_key(cfg):
+    return f"q{cfg['q']}k{cfg['k']}"
+
+
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -66,7 +70,7 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -81,7 +85,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -186,17 +190,41 @@ def run_reference(args, cfg):
 # our arm
 # ----------------------------------------------------------------------------
 
-def stage_bytes(p, es):
-    """Algorithmic bytes per launch of each single-stage measurement."""
-    L, w, B, W, R = p.loops, p.w, p.B, p.W_RLFC, p.RLFC_loops
+def stage_bytes(p, es, pf_form):
+    """Algorithmic bytes per launch of each single-stage measurement.
+
+    perm_filter: the streaming form reads every signal element once (n samples),
+    writes the RLFC sub-samples (RLFC_loops * W_RLFC) and the row-group partial
+    bins, and reads the bucket-major tap table (B * (w/B + 1) taps); the gather
+    form reads loops * w tapped samples, the w taps and writes the bins.
+    """
+    L, w, B, W, R, n = p.loops, p.w, p.B, p.W_RLFC, p.RLFC_loops, p.n
     t = es // 2
+    if pf_form["streaming"]:
+        pf = n * es + R * W * es + pf_form["row_groups"] * L * B * es + B * (w // B + 1) * es
+    else:
+        pf = L * w * es + w * es + L * B * es
     return {
-        # every tap of every loop gathers one signal element, taps read once, bins written once
-        "perm_filter": L * w * es + w * es + L * B * es,
-        # strided gather of W samples per RLFC loop + |.|^2 written; 2 passes through scratch
+        "perm_filter": pf,
+        # sub-samples read + |.|^2 written, complex data through scratch between the 2 passes
         "rlfc_fft": R * W * es + R * W * t + 2 * R * W * es,
         "bucket_fft": 2 * L * B * es * 2 + L * B * t,
     }
+
+
+def useful_bytes(p, es):
+    """Bytes the perm+filter function consumes and produces, independent of
+    the access pattern: the loops * w tapped samples, the RLFC sub-samples, the
+    taps and the bins."""
+    return p.loops * p.w * es + p.RLFC_loops * p.W_RLFC * es + p.w * es + p.loops * p.B * es
+
+
+# DRAM bytes (read + write) per launch of the dominant kernel, from the ncu
+# captures summarised under profiles/ (keyed by kernel, form and workload):
+# profiles/pf_tma_kernel_stream_perm_filter.md.
+TRAFFIC = {
+    ("perm_filter", "stream", "q27k16000"): int(1.10e9 + 28.59e6),
+}
 
 
 def run_ours(args, cfg):
@@ -329,20 +357,21 @@ def run_ours(args, cfg):
 
     # --- roofline of the dominant single-kernel stage of the mixed run
     peaks, peak_src = load_peaks()
-    sb = stage_bytes(p, 8)
+    form = plans["mixed"].describe()
+    sb = stage_bytes(p, 8, form)
     dom = max(("perm_filter", "rlfc_fft", "bucket_fft"), key=lambda s: st32.get(s, 0.0))
     achieved = sb[dom] / (st32[dom] * 1e-3) / 1e9
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        try:
-            traffic = json.load(open(tfile)).get(dom)
-        except Exception:
-            traffic = None
+    form_name = "stream" if form["streaming"] else "gather"
+    traffic = TRAFFIC.get((dom, form_name if dom == "perm_filter" else "", workload_key(cfg)))
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
             "peak": peaks["hbm_gbs"], "peak_source": peak_src, "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
-            "algorithmic_bytes_per_launch": sb[dom], "launch_ms": round(st32[dom], 4)}
+            "algorithmic_bytes_per_launch": sb[dom], "launch_ms": round(st32[dom], 4),
+            "perm_filter_form": form_name}
+    if dom == "perm_filter":
+        ub = useful_bytes(p, 8)
+        roof["useful_bytes_per_launch"] = ub
+        roof["useful_frac"] = round(ub / (st32[dom] * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)
 
     # --- CPU baseline (rank 0): the oracle on the host cores, bounded sample
     cpu = None
@@ -396,7 +425,7 @@ def run_ours(args, cfg):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gsfft", choices=["gsfft", "reference"])
     ap.add_argument("--q", type=int, default=None, help=argparse.SUPPRESS)  # smaller n for local checks

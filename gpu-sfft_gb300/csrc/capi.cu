@@ -172,6 +172,13 @@ int gsfft_plan_launches_per_run(gsfft_plan plan) {
   return plan ? plan->impl->launches_per_run : -1;
 }
 
+int gsfft_plan_describe(gsfft_plan plan, int *streaming, int *row_groups) {
+  if (!plan || !streaming || !row_groups) return GSFFT_ERR_PARAM;
+  *streaming = plan->impl->use_stream ? 1 : 0;
+  *row_groups = plan->impl->use_stream ? plan->impl->groups : 0;
+  return GSFFT_OK;
+}
+
 int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sign, int precision,
               void *stream) {
   if (!d_in || !d_out || batch < 1 || (sign != 1 && sign != -1)) return GSFFT_ERR_PARAM;

@@ -82,6 +82,7 @@ def lib():
         "gsfft_device_results": ([P, P, P, P, P], i),
         "gsfft_debug_stages": ([P, P, C.POINTER(i), P, P, P], i),
         "gsfft_plan_launches_per_run": ([P], i),
+        "gsfft_plan_describe": ([P, C.POINTER(i), C.POINTER(i)], i),
         "gsfft_plan_enable_timing": ([P, i], i),
         "gsfft_plan_stage_times": ([P, C.POINTER(C.c_float), i, C.POINTER(i)], i),
         "gsfft_stage_name": ([i], C.c_char_p),
@@ -274,3 +275,9 @@ class Plan:
 
     def launches_per_run(self):
         return lib().gsfft_plan_launches_per_run(self.h)
+
+    def describe(self):
+        """{'streaming': bool, 'row_groups': int} -- the perm+filter form chosen."""
+        st, g = C.c_int(0), C.c_int(0)
+        check(lib().gsfft_plan_describe(self.h, C.byref(st), C.byref(g)), "gsfft_plan_describe")
+        return {"streaming": bool(st.value), "row_groups": g.value}

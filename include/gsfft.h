@@ -139,6 +139,11 @@ const char *gsfft_stage_name(int stage);
 /* Number of kernel launches one gsfft_run issues for this plan. */
 int gsfft_plan_launches_per_run(gsfft_plan plan);
 
+/* Form of the perm+filter stage the plan chose: *streaming = 1 when it
+ * streams the whole signal once (with *row_groups partial bin sets), 0 when
+ * it gathers the loops*w tapped samples. */
+int gsfft_plan_describe(gsfft_plan plan, int *streaming, int *row_groups);
+
 /* ---- building blocks (also used by the stage drop-ins) ------------------ */
 
 /* Batched unnormalised complex FFT of power-of-two size n_fft >= 256,

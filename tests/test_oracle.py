@@ -1,23 +1,30 @@
 """CPU checks of the oracle (oracle/sfft_oracle.c) against the reference's
 published known answers (README.md:84-90) and against small pure-Python
 restatements of the reference stages.  No GPU needed."""
+import json
 import math
+import os
 
 import numpy as np
 import pytest
 
 from gsfft import synth
 
-# README.md:84-90: `./exec 27 16000 0.65 2 2 7 4096 2` prints these values.
-README_KAT = dict(B_thresh=32000, W_RLFC=4194304, b_f=966, B=131072, w=2230607, BB=183314.0)
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "readme_kats.json")
 
 
 def test_params_readme_kat(O):
-    p, st = O.derive_params(27, 16000, 0.65, 2, 2, 7, 4096, 2)
+    """README.md:80-92: `./exec 27 16000 0.65 2 2 7 4096 2` prints these values."""
+    kat = json.load(open(GOLDEN))
+    a = kat["args"]
+    p, st = O.derive_params(a["q"], a["k"], a["Bcst"], a["loops_loc"], a["loops_thresh"],
+                            a["loops_est"], a["RLFC_cst"], a["RLFC_loops"])
     assert st == 0
-    for k, v in README_KAT.items():
-        assert getattr(p, k) == v, k
-    assert 0.5 / p.lobefrac == 183314.0  # "numlobes=183314.0"
+    e = kat["expect"]
+    for key in ("RLFC_loops", "B_thresh", "W_RLFC", "b_f", "B", "w", "tolerance"):
+        assert getattr(p, key) == e[key], key
+    assert 0.5 / p.lobefrac == e["numlobes"]  # "numlobes=183314.0"
+    assert p.BB == e["numlobes"]
     assert p.loops == 9 and p.n == 1 << 27
 
 
