@@ -172,6 +172,58 @@ int gsfft_plan_launches_per_run(gsfft_plan plan) {
   return plan ? plan->impl->launches_per_run : -1;
 }
 
+/* ---------------------------------------------------------------- host I/O */
+
+static int sync_check(cudaStream_t st, const char *what);
+
+int gsfft_alloc(void **d_ptr, size_t bytes) {
+  if (!d_ptr) return GSFFT_ERR_PARAM;
+  *d_ptr = nullptr;
+  if (bytes == 0) return GSFFT_OK;
+  const cudaError_t e = cudaMalloc(d_ptr, bytes);
+  if (e != cudaSuccess) {
+    set_last_error("gsfft_alloc(%zu): %s", bytes, cudaGetErrorString(e));
+    *d_ptr = nullptr;
+    return GSFFT_ERR_ALLOC;
+  }
+  return GSFFT_OK;
+}
+
+int gsfft_free(void *d_ptr) {
+  if (d_ptr && cudaFree(d_ptr) != cudaSuccess) {
+    set_last_error("gsfft_free: %s", cudaGetErrorString(cudaGetLastError()));
+    return GSFFT_ERR_CUDA;
+  }
+  return GSFFT_OK;
+}
+
+int gsfft_copy(void *dst, const void *src, size_t bytes, void *stream) {
+  if ((!dst || !src) && bytes) return GSFFT_ERR_PARAM;
+  if (bytes == 0) return GSFFT_OK;
+  GS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, S(stream)));
+  return sync_check(S(stream), "gsfft_copy");
+}
+
+int gsfft_ingest(const complex_t *h_x, long long n, int precision, void *d_x, void *stream) {
+  if (!h_x || !d_x || n < 1 || (precision != GSFFT_FP64 && precision != GSFFT_MIXED))
+    return GSFFT_ERR_PARAM;
+  return ingest(h_x, n, precision, d_x, S(stream));
+}
+
+int gsfft_convert_signal(const complex_t *d_in, void *d_out, long long n, void *stream) {
+  if (!d_in || !d_out || n < 1) return GSFFT_ERR_PARAM;
+  return launch_to_float(d_in, d_out, n, S(stream));
+}
+
+int gsfft_sync(void *stream) { return sync_check(S(stream), "gsfft_sync"); }
+
+int gsfft_evaluate(gsfft_plan plan, const complex_t *d_x_f, const int *d_true_loc, int k_true,
+                   int *missed_estimation, int *missed_result, double *mse_k, void *stream) {
+  if (!plan || !d_x_f || (!d_true_loc && k_true) || k_true < 0) return GSFFT_ERR_PARAM;
+  return plan_evaluate(plan->impl, d_x_f, d_true_loc, k_true, missed_estimation, missed_result,
+                       mse_k, S(stream));
+}
+
 int gsfft_plan_describe(gsfft_plan plan, int *streaming, int *row_groups) {
   if (!plan || !streaming || !row_groups) return GSFFT_ERR_PARAM;
   *streaming = plan->impl->use_stream ? 1 : 0;

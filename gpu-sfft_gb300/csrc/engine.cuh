@@ -68,6 +68,12 @@ int plan_debug(Plan *P, int *h_J2, int *num_RLFC, int *h_J, void *h_bins, cudaSt
 int launch_hinv(const double2 *d_ff, int n, int nb, double2 *hinv, cudaStream_t st);
 int launch_convert_taps(const double2 *d_ft, void *dst, int w, bool to_float, cudaStream_t st);
 
+// signal ingest and device-side evaluation (host_io.cu)
+int launch_to_float(const complex_t *in, void *out, long long n, cudaStream_t st);
+int ingest(const complex_t *h_x, long long n, int precision, void *d_x, cudaStream_t st);
+int plan_evaluate(Plan *P, const complex_t *d_xf, const int *d_true_loc, int k_true,
+                  int *missed_est, int *missed_res, double *err, cudaStream_t st);
+
 // A2 filter design on the GPU
 int design_filter(const gsfft_params &p, double2 *d_ft, double2 *d_ff, cudaStream_t st);
 

@@ -83,6 +83,13 @@ def lib():
         "gsfft_debug_stages": ([P, P, C.POINTER(i), P, P, P], i),
         "gsfft_plan_launches_per_run": ([P], i),
         "gsfft_plan_describe": ([P, C.POINTER(i), C.POINTER(i)], i),
+        "gsfft_alloc": ([C.POINTER(P), C.c_size_t], i),
+        "gsfft_free": ([P], i),
+        "gsfft_copy": ([P, P, C.c_size_t, P], i),
+        "gsfft_sync": ([P], i),
+        "gsfft_ingest": ([P, ll, i, P, P], i),
+        "gsfft_convert_signal": ([P, P, ll, P], i),
+        "gsfft_evaluate": ([P, P, P, i, C.POINTER(i), C.POINTER(i), C.POINTER(d), P], i),
         "gsfft_plan_enable_timing": ([P, i], i),
         "gsfft_plan_stage_times": ([P, C.POINTER(C.c_float), i, C.POINTER(i)], i),
         "gsfft_stage_name": ([i], C.c_char_p),
@@ -155,6 +162,17 @@ def fft(d_in, d_out, n, batch=1, sign=-1, precision=FP64, stream=0):
 def cutoff(d_samples, size, num, batch, precision, d_out, stream=0):
     check(lib().gsfft_cutoff(d_samples, size, num, batch, precision, d_out, stream or None),
           "gsfft_cutoff")
+
+
+def ingest(h_x, precision, d_x, stream=0):
+    """Host complex128 signal -> device (complex128 for FP64, complex64 for MIXED)."""
+    h_x = np.ascontiguousarray(h_x, dtype=np.complex128)
+    check(lib().gsfft_ingest(_np_ptr(h_x), h_x.size, precision, d_x, stream or None), "gsfft_ingest")
+    check(lib().gsfft_sync(stream or None), "gsfft_sync")
+
+
+def convert_signal(d_in, d_out, n, stream=0):
+    check(lib().gsfft_convert_signal(d_in, d_out, n, stream or None), "gsfft_convert_signal")
 
 
 # limits of cutoff_noalloc (GSFFT_NOALLOC_MAX_SIZE / _BATCH in gsfft.h)
@@ -275,6 +293,14 @@ class Plan:
 
     def launches_per_run(self):
         return lib().gsfft_plan_launches_per_run(self.h)
+
+    def evaluate(self, d_x_f, d_true_loc, k_true, stream=0):
+        """Device-side MISSED (estimation, result) and MSE*k of the last run
+        (d_true_loc: ascending distinct locations)."""
+        me, mr, e = C.c_int(0), C.c_int(0), C.c_double(0.0)
+        check(lib().gsfft_evaluate(self.h, d_x_f, d_true_loc, k_true, C.byref(me), C.byref(mr),
+                                   C.byref(e), stream or None), "gsfft_evaluate")
+        return {"missed_estimation": me.value, "missed_result": mr.value, "mse_k": e.value}
 
     def describe(self):
         """{'streaming': bool, 'row_groups': int} -- the perm+filter form chosen."""

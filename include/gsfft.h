@@ -15,6 +15,8 @@
 #ifndef GSFFT_H_
 #define GSFFT_H_
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -143,6 +145,37 @@ int gsfft_plan_launches_per_run(gsfft_plan plan);
  * streams the whole signal once (with *row_groups partial bin sets), 0 when
  * it gathers the loops*w tapped samples. */
 int gsfft_plan_describe(gsfft_plan plan, int *streaming, int *row_groups);
+
+/* ---- host I/O and evaluation ---------------------------------------- */
+
+/* Device memory and copies for callers that do not link the CUDA runtime
+ * themselves (the command-line driver).  gsfft_copy copies in any direction
+ * (unified addressing) and waits for stream. */
+int gsfft_alloc(void **d_ptr, size_t bytes);
+int gsfft_free(void *d_ptr);
+int gsfft_copy(void *dst, const void *src, size_t bytes, void *stream);
+int gsfft_sync(void *stream);
+
+/* Signal ingest (replaces the synchronous host-to-device copy of
+ * cuExperiment.cu:113-122): n complex_t samples from host memory into d_x,
+ * as complex_t (FP64) or converted to {float, float} on the device (MIXED).
+ * Pageable memory goes through two pinned 32 MiB staging chunks so the CPU
+ * copy overlaps the DMA; pinned FP64 input is copied directly.  Queued on
+ * stream (returns once the last chunk is queued); the staging buffers are
+ * created on the first call and kept for the process. */
+int gsfft_ingest(const complex_t *h_x, long long n, int precision, void *d_x, void *stream);
+/* FP64 -> FP32 conversion of a device signal (n complex samples). */
+int gsfft_convert_signal(const complex_t *d_in, void *d_out, long long n, void *stream);
+
+/* Device-side evaluation of the plan's last run (run_experiment,
+ * cuExperiment.cu:178-216): missed_estimation = true locations that are not
+ * candidates, missed_result = true locations not among the k largest,
+ * mse_k = sum over all n bins of |xhat_k - x_f|^2, where x_f (n complex_t on
+ * the device) is the normalised DFT of the signal and xhat_k holds the k
+ * largest estimates.  d_true_loc: the k_true true locations, ascending and
+ * distinct.  Synchronises stream. */
+int gsfft_evaluate(gsfft_plan plan, const complex_t *d_x_f, const int *d_true_loc, int k_true,
+                   int *missed_estimation, int *missed_result, double *mse_k, void *stream);
 
 /* ---- building blocks (also used by the stage drop-ins) ------------------ */
 
