@@ -422,6 +422,154 @@ def run_ours(args, cfg):
     return 0
 
 
+# ----------------------------------------------------------------------------
+# further configurations (not the headline line): noisy, batched, large-k
+# ----------------------------------------------------------------------------
+
+def _plan_for(gsfft, torch, p, prec, dev, flags=0):
+    d_ft = torch.zeros(p.w, dtype=torch.complex128, device=dev)
+    d_ff = torch.zeros(p.n, dtype=torch.complex128, device=dev)
+    gsfft.design_filter(p, d_ft.data_ptr(), d_ff.data_ptr())
+    plan = gsfft.Plan(p, prec, flags)
+    plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+    del d_ft, d_ff
+    return plan
+
+
+def _rel_l2_common(r64, r32):
+    k64 = r64["topk"]["key"].tolist()
+    v64 = dict(zip(k64, r64["topk"]["x"] + 1j * r64["topk"]["y"]))
+    k32 = r32["topk"]["key"].tolist()
+    v32 = dict(zip(k32, r32["topk"]["x"] + 1j * r32["topk"]["y"]))
+    common = [kk for kk in k32 if kk in v64]
+    a64 = np.array([v64[kk] for kk in common])
+    a32 = np.array([v32[kk] for kk in common])
+    return set(k64) == set(k32), float(np.linalg.norm(a32 - a64) / max(np.linalg.norm(a64), 1e-300))
+
+
+def run_configs(args):
+    """Noisy (n=2^27, k=16000, 40 dB), batched (256 signals, q in 18..24,
+    k log-uniform in [50, 4000], Bcst in [0.6, 1.5]) and large-k (8 signals
+    n=2^27, k=43000, 30 dB) measurements; one JSON line each."""
+    import torch
+    import gsfft
+    from gsfft import synth
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    gsfft.lib()
+    st = torch.cuda.current_stream(dev)
+    sh = st.cuda_stream
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    if args.workload == "noisy40":
+        cfg = dict(CFG)
+        p, _ = gsfft.derive_params(*cfg_args(cfg))
+        x64, loc, coef, X = synth.signal_torch(p.n, p.k, seed=3, snr_db=40.0, device=dev)
+        x32 = x64.to(torch.complex64)
+        plans = {"fp64": _plan_for(gsfft, torch, p, gsfft.FP64, dev),
+                 "mixed": _plan_for(gsfft, torch, p, gsfft.MIXED, dev)}
+        dr = synth.draws(3, p.n, p.W_RLFC, p.RLFC_loops, p.loops)
+        ms = {name: timed(lambda pl=pl, xx=(x64 if name == "fp64" else x32):
+                          pl.run(xx.data_ptr(), *dr, stream=sh), args.steps)
+              for name, pl in plans.items()}
+        res = {name: pl.results(stream=sh) for name, pl in plans.items()}
+        same, rel = _rel_l2_common(res["fp64"], res["mixed"])
+        tl = torch.as_tensor(np.sort(np.asarray(loc, np.int32)), device=dev)
+        ev = {name: pl.evaluate(X.data_ptr(), tl.data_ptr(), tl.numel()) for name, pl in plans.items()}
+        line = {"workload": "noisy40", "metric": "sparse FFTs/sec at n=2^27,k=16000, 40 dB",
+                "unit": UNIT, "value": 1e3 / ms["mixed"], "fp64_value": 1e3 / ms["fp64"],
+                "mixed_over_fp64": ms["fp64"] / ms["mixed"], "same_location_set": same,
+                "mixed_vs_fp64_rel_l2": rel,
+                "vs_full_fft": {kk: {"missed_result": v["missed_result"],
+                                     "rel_l2": float(np.sqrt(v["mse_k"] / p.k))} for kk, v in ev.items()}}
+    elif args.workload == "batched256":
+        rng = np.random.default_rng(2024)
+        plans, xs, drs, qs = [], [], [], []
+        while len(plans) < 256:
+            q = int(rng.integers(18, 25))
+            k = int(round(float(np.exp(rng.uniform(np.log(50), np.log(4000))))))
+            bc = float(rng.uniform(0.6, 1.5))
+            p, stt = gsfft.derive_params(q, k, bc, 2, 2, 5, 128, 2)
+            if stt != 0:
+                continue  # the reference would assert: draw again
+            try:
+                pl = _plan_for(gsfft, torch, p, gsfft.MIXED, dev)
+            except RuntimeError:
+                continue  # a window layout this engine rejects: draw again
+            seed = len(plans)
+            x64, _, _, _ = synth.signal_torch(p.n, p.k, seed=seed, device=dev)
+            xs.append(x64.to(torch.complex64))
+            del x64
+            plans.append(pl)
+            drs.append(synth.draws(seed, p.n, p.W_RLFC, p.RLFC_loops, p.loops))
+            qs.append(q)
+        batch = gsfft.Batch(plans, streams=16)
+        ptrs = [x.data_ptr() for x in xs]
+        ms_b = timed(lambda: batch.run(ptrs, drs, stream=sh), args.steps)
+
+        def seq():
+            for pl, x, d in zip(plans, xs, drs):
+                pl.run(x.data_ptr(), *d, stream=sh)
+        ms_s = timed(seq, max(1, args.steps // 4))
+        line = {"workload": "batched256", "metric": "sparse FFTs/sec, 256 mixed signals q=18..24",
+                "unit": UNIT, "value": 256e3 / ms_b, "sequential_value": 256e3 / ms_s,
+                "ms_per_batch": ms_b, "signals_by_q": {str(q): qs.count(q) for q in range(18, 25)}}
+        batch.close()
+    else:  # largek8
+        p, stt = gsfft.derive_params(27, 43000, 0.8, 3, 2, 8, 32768, 2)
+        assert stt == 0
+        plans, xs, drs, truth = [], [], [], []
+        d_ft = torch.zeros(p.w, dtype=torch.complex128, device=dev)
+        d_ff = torch.zeros(p.n, dtype=torch.complex128, device=dev)
+        gsfft.design_filter(p, d_ft.data_ptr(), d_ff.data_ptr())
+        for i in range(8):
+            pl = gsfft.Plan(p, gsfft.MIXED, 0)
+            pl.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+            x64, loc, coef, X = synth.signal_torch(p.n, p.k, seed=50 + i, snr_db=30.0, device=dev)
+            xs.append(x64.to(torch.complex64))
+            if i == 0:
+                x0_64, X0, loc0 = x64, X, loc
+            del x64
+            plans.append(pl)
+            drs.append(synth.draws(50 + i, p.n, p.W_RLFC, p.RLFC_loops, p.loops))
+        batch = gsfft.Batch(plans, streams=4)
+        ptrs = [x.data_ptr() for x in xs]
+        ms_b = timed(lambda: batch.run(ptrs, drs, stream=sh), args.steps)
+        # accuracy of signal 0: mixed vs FP64 and both vs the full FFT
+        p64 = gsfft.Plan(p, gsfft.FP64, 0)
+        p64.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+        ms_64 = timed(lambda: p64.run(x0_64.data_ptr(), *drs[0], stream=sh), max(1, args.steps // 2))
+        plans[0].run(xs[0].data_ptr(), *drs[0], stream=sh)
+        r32, r64 = plans[0].results(stream=sh), p64.results(stream=sh)
+        same, rel = _rel_l2_common(r64, r32)
+        tl = torch.as_tensor(np.sort(np.asarray(loc0, np.int32)), device=dev)
+        ev32 = plans[0].evaluate(X0.data_ptr(), tl.data_ptr(), tl.numel())
+        ev64 = p64.evaluate(X0.data_ptr(), tl.data_ptr(), tl.numel())
+        line = {"workload": "largek8", "metric": "sparse FFTs/sec, 8 mixed signals n=2^27 k=43000 30 dB",
+                "unit": UNIT, "value": 8e3 / ms_b, "ms_per_batch": ms_b, "fp64_single_value": 1e3 / ms_64,
+                "same_location_set": same, "mixed_vs_fp64_rel_l2": rel,
+                "vs_full_fft": {"mixed": {"missed_result": ev32["missed_result"],
+                                          "rel_l2": float(np.sqrt(ev32["mse_k"] / p.k))},
+                                "fp64": {"missed_result": ev64["missed_result"],
+                                         "rel_l2": float(np.sqrt(ev64["mse_k"] / p.k))}}}
+        batch.close()
+        p64.close()
+    line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic"})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -430,7 +578,8 @@ def main():
     ap.add_argument("--impl", default="gsfft", choices=["gsfft", "reference"])
     ap.add_argument("--q", type=int, default=None, help=argparse.SUPPRESS)  # smaller n for local checks
     ap.add_argument("--skip-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="headline", choices=["headline", "small"],
+    ap.add_argument("--workload", default="headline",
+                    choices=["headline", "small", "noisy40", "batched256", "largek8"],
                     help="small: n=2^25, k=4000 (same W_RLFC) for profiler captures")
     ap.add_argument("--pf", default="auto", choices=["auto", "gather", "stream"],
                     help="perm+filter form (auto: by the plan's DRAM byte model)")
@@ -446,6 +595,8 @@ def main():
         cfg.update(q=args.q, k=1000, Bcst=1.40, loops_est=5, RLFC_cst=128)
     if args.impl == "reference":
         return run_reference(args, cfg)
+    if args.workload in ("noisy40", "batched256", "largek8"):
+        return run_configs(args)
     return run_ours(args, cfg)
 
 

@@ -1,0 +1,85 @@
+// Batched runs: many plans (signals with their own n, k and parameters) in
+// one call.  The batch forks the caller's stream into a fixed set of internal
+// streams, runs plan i's pipeline on stream i mod S, and joins them back, so
+// the small transforms of different signals fill the GPU together instead of
+// one after the other.  Plans keep their own buffers (nothing is shared
+// between concurrently running pipelines), so the results of a batched run
+// are identical to running each plan alone.
+#include "engine.cuh"
+
+#include <vector>
+
+namespace gsfft {
+
+static_assert(GSFFT_MAX_LOOPS == MAX_LOOPS && GSFFT_MAX_RLFC_LOOPS == MAX_RLFC_LOOPS,
+              "draw strides of gsfft_run_batched");
+
+struct Batch {
+  std::vector<Plan *> plans;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+};
+
+void batch_destroy(Batch *b) {
+  if (!b) return;
+  for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  delete b;
+}
+
+int batch_create(Plan *const *plans, int count, int nstreams, Batch **out) {
+  if (!plans || count < 1 || !out) return GSFFT_ERR_PARAM;
+  for (int i = 0; i < count; i++)
+    if (!plans[i]) return GSFFT_ERR_PARAM;
+  Batch *b = new Batch();
+  b->plans.assign(plans, plans + count);
+  const int S = nstreams < 1 ? 1 : (nstreams > count ? count : nstreams);
+  int s = GSFFT_OK;
+  for (int i = 0; i < S && s == GSFFT_OK; i++) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      if (st) cudaStreamDestroy(st);
+      set_last_error("gsfft_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
+      s = GSFFT_ERR_CUDA;
+      break;
+    }
+    b->streams.push_back(st);
+    b->joins.push_back(ev);
+  }
+  if (s == GSFFT_OK && cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+    s = GSFFT_ERR_CUDA;
+  if (s != GSFFT_OK) {
+    batch_destroy(b);
+    return s;
+  }
+  *out = b;
+  return GSFFT_OK;
+}
+
+int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, const int *ai,
+              cudaStream_t st) {
+  if (!b || !d_x || !offs || !a || !ai) return GSFFT_ERR_PARAM;
+  const int S = (int)b->streams.size();
+  GS_CUDA(cudaEventRecord(b->fork, st));
+  for (int i = 0; i < S; i++) GS_CUDA(cudaStreamWaitEvent(b->streams[i], b->fork, 0));
+  const int n = (int)b->plans.size();
+  int s = GSFFT_OK;
+  for (int i = 0; i < n && s == GSFFT_OK; i++)
+    s = plan_run(b->plans[i], d_x[i], offs + (size_t)i * MAX_RLFC_LOOPS, a + (size_t)i * MAX_LOOPS,
+                 ai + (size_t)i * MAX_LOOPS, b->streams[i % S]);
+  // join every internal stream back into the caller's stream, also on error
+  for (int i = 0; i < S; i++) {
+    if (cudaEventRecord(b->joins[i], b->streams[i]) != cudaSuccess ||
+        cudaStreamWaitEvent(st, b->joins[i], 0) != cudaSuccess) {
+      set_last_error("gsfft_run_batched: join: %s", cudaGetErrorString(cudaGetLastError()));
+      if (s == GSFFT_OK) s = GSFFT_ERR_CUDA;
+    }
+  }
+  return s;
+}
+
+}  // namespace gsfft

@@ -6,6 +6,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 namespace gsfft {
 
 thread_local int g_launch_counter = 0;
@@ -170,6 +172,39 @@ const char *gsfft_stage_name(int stage) { return stage_name(stage); }
 
 int gsfft_plan_launches_per_run(gsfft_plan plan) {
   return plan ? plan->impl->launches_per_run : -1;
+}
+
+/* ---------------------------------------------------------------- batches */
+
+struct gsfft_batch_s {
+  Batch *impl;
+};
+
+int gsfft_batch_create(const gsfft_plan *plans, int count, int streams, gsfft_batch *out) {
+  if (!plans || count < 1 || !out) return GSFFT_ERR_PARAM;
+  std::vector<Plan *> ps((size_t)count);
+  for (int i = 0; i < count; i++) {
+    if (!plans[i]) return GSFFT_ERR_PARAM;
+    ps[(size_t)i] = plans[i]->impl;
+  }
+  Batch *b = nullptr;
+  const int s = batch_create(ps.data(), count, streams, &b);
+  if (s != GSFFT_OK) return s;
+  *out = new gsfft_batch_s{b};
+  return GSFFT_OK;
+}
+
+int gsfft_batch_destroy(gsfft_batch batch) {
+  if (!batch) return GSFFT_ERR_PARAM;
+  batch_destroy(batch->impl);
+  delete batch;
+  return GSFFT_OK;
+}
+
+int gsfft_run_batched(gsfft_batch batch, const void *const *d_x, const int *h_rlfc_offsets,
+                      const int *h_a, const int *h_ai, void *stream) {
+  if (!batch) return GSFFT_ERR_PARAM;
+  return batch_run(batch->impl, d_x, h_rlfc_offsets, h_a, h_ai, S(stream));
 }
 
 /* ---------------------------------------------------------------- host I/O */

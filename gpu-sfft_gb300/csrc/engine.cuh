@@ -68,6 +68,13 @@ int plan_debug(Plan *P, int *h_J2, int *num_RLFC, int *h_J, void *h_bins, cudaSt
 int launch_hinv(const double2 *d_ff, int n, int nb, double2 *hinv, cudaStream_t st);
 int launch_convert_taps(const double2 *d_ft, void *dst, int w, bool to_float, cudaStream_t st);
 
+// batched runs over several plans (batch.cu)
+struct Batch;
+int batch_create(Plan *const *plans, int count, int nstreams, Batch **out);
+int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, const int *ai,
+              cudaStream_t st);
+void batch_destroy(Batch *b);
+
 // signal ingest and device-side evaluation (host_io.cu)
 int launch_to_float(const complex_t *in, void *out, long long n, cudaStream_t st);
 int ingest(const complex_t *h_x, long long n, int precision, void *d_x, cudaStream_t st);

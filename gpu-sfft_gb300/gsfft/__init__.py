@@ -83,6 +83,9 @@ def lib():
         "gsfft_debug_stages": ([P, P, C.POINTER(i), P, P, P], i),
         "gsfft_plan_launches_per_run": ([P], i),
         "gsfft_plan_describe": ([P, C.POINTER(i), C.POINTER(i)], i),
+        "gsfft_batch_create": ([C.POINTER(P), i, i, C.POINTER(P)], i),
+        "gsfft_batch_destroy": ([P], i),
+        "gsfft_run_batched": ([P, C.POINTER(P), P, P, P, P], i),
         "gsfft_alloc": ([C.POINTER(P), C.c_size_t], i),
         "gsfft_free": ([P], i),
         "gsfft_copy": ([P, P, C.c_size_t, P], i),
@@ -162,6 +165,46 @@ def fft(d_in, d_out, n, batch=1, sign=-1, precision=FP64, stream=0):
 def cutoff(d_samples, size, num, batch, precision, d_out, stream=0):
     check(lib().gsfft_cutoff(d_samples, size, num, batch, precision, d_out, stream or None),
           "gsfft_cutoff")
+
+
+MAX_LOOPS = 32        # GSFFT_MAX_LOOPS
+MAX_RLFC_LOOPS = 8    # GSFFT_MAX_RLFC_LOOPS
+
+
+class Batch:
+    """gsfft_batch over existing Plan objects (kept alive by the batch)."""
+
+    def __init__(self, plans, streams=8):
+        self.plans = list(plans)
+        arr = (C.c_void_p * len(self.plans))(*[pl.h for pl in self.plans])
+        h = C.c_void_p()
+        check(lib().gsfft_batch_create(arr, len(self.plans), streams, C.byref(h)), "gsfft_batch_create")
+        self.h = h
+
+    def run(self, d_xs, draws, stream=0):
+        """d_xs: device pointers, draws: per plan (offsets, a, ai)."""
+        n = len(self.plans)
+        offs = np.zeros((n, MAX_RLFC_LOOPS), np.int32)
+        a = np.zeros((n, MAX_LOOPS), np.int32)
+        ai = np.zeros((n, MAX_LOOPS), np.int32)
+        for i, (o, aa, ii) in enumerate(draws):
+            offs[i, :len(o)] = o
+            a[i, :len(aa)] = aa
+            ai[i, :len(ii)] = ii
+        xs = (C.c_void_p * n)(*[int(v) for v in d_xs])
+        check(lib().gsfft_run_batched(self.h, xs, _np_ptr(offs), _np_ptr(a), _np_ptr(ai),
+                                      stream or None), "gsfft_run_batched")
+
+    def close(self):
+        if self.h:
+            lib().gsfft_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ingest(h_x, precision, d_x, stream=0):

@@ -146,6 +146,29 @@ int gsfft_plan_launches_per_run(gsfft_plan plan);
  * it gathers the loops*w tapped samples. */
 int gsfft_plan_describe(gsfft_plan plan, int *streaming, int *row_groups);
 
+/* ---- batches --------------------------------------------------------- */
+
+/* Strides of the per-plan draw arrays of gsfft_run_batched. */
+#define GSFFT_MAX_LOOPS 32
+#define GSFFT_MAX_RLFC_LOOPS 8
+
+typedef struct gsfft_batch_s *gsfft_batch;
+
+/* A batch of existing plans (any mix of n, k, parameters and precisions;
+ * each plan with its filter installed).  streams: internal CUDA streams the
+ * runs are spread over (plan i on stream i mod streams).  The plans stay
+ * owned by the caller and must outlive the batch. */
+int gsfft_batch_create(const gsfft_plan *plans, int count, int streams, gsfft_batch *out);
+int gsfft_batch_destroy(gsfft_batch batch);
+
+/* One sparse FFT per plan: plan i transforms d_x[i] with the draws
+ * h_rlfc_offsets[i * GSFFT_MAX_RLFC_LOOPS + r], h_a[i * GSFFT_MAX_LOOPS + l],
+ * h_ai[i * GSFFT_MAX_LOOPS + l].  Forks from stream and joins back into it
+ * (asynchronous); each plan's results are then read with gsfft_get_results
+ * and equal those of gsfft_run on the same input and draws. */
+int gsfft_run_batched(gsfft_batch batch, const void *const *d_x, const int *h_rlfc_offsets,
+                      const int *h_a, const int *h_ai, void *stream);
+
 /* ---- host I/O and evaluation ---------------------------------------- */
 
 /* Device memory and copies for callers that do not link the CUDA runtime

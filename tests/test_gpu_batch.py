@@ -1,0 +1,52 @@
+"""gsfft_run_batched: a batch of plans with different sizes, parameters and
+precisions gives exactly the results of running each plan alone."""
+import numpy as np
+import pytest
+
+from gsfft import synth
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # (q, k, Bcst, loops_loc, loops_thresh, loops_est, RLFC_cst, RLFC_loops), precision
+    ((14, 10, 2.5, 2, 2, 5, 16, 2), 0),
+    ((16, 20, 1.0, 2, 2, 5, 8, 2), 1),
+    ((18, 100, 1.0, 3, 2, 6, 32, 2), 1),
+    ((16, 40, 1.2, 2, 2, 4, 16, 2), 0),
+    ((20, 1000, 1.40, 2, 2, 5, 128, 2), 1),
+    ((18, 60, 0.9, 2, 2, 5, 32, 2), 0),
+]
+
+
+def _setup(G, torch, cfg, prec, seed):
+    p, st = G.derive_params(*cfg)
+    assert st == 0
+    d_ft = torch.zeros(p.w, dtype=torch.complex128, device="cuda")
+    d_ff = torch.zeros(p.n, dtype=torch.complex128, device="cuda")
+    G.design_filter(p, d_ft.data_ptr(), d_ff.data_ptr())
+    plan = G.Plan(p, prec, 0)
+    plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+    x, loc, coef, X = synth.signal_numpy(p.n, p.k, seed=seed)
+    d_x = torch.from_numpy(x.astype(np.complex128 if prec == 0 else np.complex64)).cuda()
+    draws = synth.draws(seed, p.n, p.W_RLFC, p.RLFC_loops, p.loops)
+    return plan, d_x, draws, (d_ft, d_ff)
+
+
+@pytest.mark.parametrize("streams", [1, 4])
+def test_batched_equals_single(G, torch_cuda, streams):
+    torch = torch_cuda
+    items = [_setup(G, torch, cfg, prec, 100 + i) for i, (cfg, prec) in enumerate(CASES)]
+    single = []
+    for plan, d_x, draws, _ in items:
+        plan.run(d_x.data_ptr(), *draws)
+        single.append(plan.results())
+    batch = G.Batch([it[0] for it in items], streams=streams)
+    batch.run([it[1].data_ptr() for it in items], [it[2] for it in items])
+    torch.cuda.synchronize()
+    for (plan, _, _, _), ref in zip(items, single):
+        got = plan.results()
+        assert got["I_F"] == ref["I_F"]
+        np.testing.assert_array_equal(got["nodes"], ref["nodes"])
+        np.testing.assert_array_equal(got["topk"], ref["topk"])
+    batch.close()
+    for it in items:
+        it[0].close()
