@@ -5,6 +5,13 @@
 // one after the other.  Plans keep their own buffers (nothing is shared
 // between concurrently running pipelines), so the results of a batched run
 // are identical to running each plan alone.
+//
+// Graph form: gsfft_batch_capture records one batched run (draws fixed at
+// capture time) into a CUDA graph; each gsfft_batch_launch replays it with one
+// launch, on whatever signals the captured d_x buffers hold by then.  Every
+// run's first kernel advances its plan's device epoch, so replays count votes
+// afresh; the host mirrors the epoch and clears a vote table before a replay
+// would wrap it.
 #include "engine.cuh"
 
 #include <vector>
@@ -19,10 +26,14 @@ struct Batch {
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> joins;
   cudaEvent_t fork = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
 };
 
 void batch_destroy(Batch *b) {
   if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
   for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
   for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
@@ -61,7 +72,7 @@ int batch_create(Plan *const *plans, int count, int nstreams, Batch **out) {
 }
 
 int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, const int *ai,
-              cudaStream_t st) {
+              cudaStream_t st, bool capturing) {
   if (!b || !d_x || !offs || !a || !ai) return GSFFT_ERR_PARAM;
   const int S = (int)b->streams.size();
   GS_CUDA(cudaEventRecord(b->fork, st));
@@ -70,7 +81,7 @@ int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, c
   int s = GSFFT_OK;
   for (int i = 0; i < n && s == GSFFT_OK; i++)
     s = plan_run(b->plans[i], d_x[i], offs + (size_t)i * MAX_RLFC_LOOPS, a + (size_t)i * MAX_LOOPS,
-                 ai + (size_t)i * MAX_LOOPS, b->streams[i % S]);
+                 ai + (size_t)i * MAX_LOOPS, b->streams[i % S], capturing);
   // join every internal stream back into the caller's stream, also on error
   for (int i = 0; i < S; i++) {
     if (cudaEventRecord(b->joins[i], b->streams[i]) != cudaSuccess ||
@@ -80,6 +91,56 @@ int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, c
     }
   }
   return s;
+}
+
+int batch_capture(Batch *b, const void *const *d_x, const int *offs, const int *a, const int *ai) {
+  if (!b || !d_x || !offs || !a || !ai) return GSFFT_ERR_PARAM;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaStream_t cs = nullptr;
+  GS_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  int s = GSFFT_OK;
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    set_last_error("gsfft_batch_capture: %s", cudaGetErrorString(cudaGetLastError()));
+    s = GSFFT_ERR_CUDA;
+  } else {
+    s = batch_run(b, d_x, offs, a, ai, cs, true);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cs, &g);
+    if (s == GSFFT_OK && e != cudaSuccess) {
+      set_last_error("gsfft_batch_capture: end capture: %s", cudaGetErrorString(e));
+      s = GSFFT_ERR_UNSUPPORTED;
+    }
+    if (s == GSFFT_OK) {
+      const cudaError_t ei = cudaGraphInstantiate(&b->exec, g, 0);
+      if (ei != cudaSuccess) {
+        set_last_error("gsfft_batch_capture: instantiate: %s", cudaGetErrorString(ei));
+        s = GSFFT_ERR_UNSUPPORTED;
+        cudaGraphDestroy(g);
+      } else {
+        b->graph = g;
+      }
+    } else if (g) {
+      cudaGraphDestroy(g);
+    }
+  }
+  cudaGetLastError();  // a failed capture leaves its error behind
+  cudaStreamDestroy(cs);
+  return s;
+}
+
+int batch_launch(Batch *b, cudaStream_t st) {
+  if (!b) return GSFFT_ERR_PARAM;
+  if (!b->exec) return GSFFT_ERR_STATE;
+  for (Plan *P : b->plans) GS_CHECK(plan_epoch_advance(P, st));
+  GS_CUDA(cudaGraphLaunch(b->exec, st));
+  return GSFFT_OK;
 }
 
 }  // namespace gsfft

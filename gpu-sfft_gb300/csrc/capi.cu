@@ -207,6 +207,17 @@ int gsfft_run_batched(gsfft_batch batch, const void *const *d_x, const int *h_rl
   return batch_run(batch->impl, d_x, h_rlfc_offsets, h_a, h_ai, S(stream));
 }
 
+int gsfft_batch_capture(gsfft_batch batch, const void *const *d_x, const int *h_rlfc_offsets,
+                        const int *h_a, const int *h_ai) {
+  if (!batch) return GSFFT_ERR_PARAM;
+  return batch_capture(batch->impl, d_x, h_rlfc_offsets, h_a, h_ai);
+}
+
+int gsfft_batch_launch(gsfft_batch batch, void *stream) {
+  if (!batch) return GSFFT_ERR_PARAM;
+  return batch_launch(batch->impl, S(stream));
+}
+
 /* ---------------------------------------------------------------- host I/O */
 
 static int sync_check(cudaStream_t st, const char *what);
@@ -393,14 +404,15 @@ int gsfft_stage_reverse_hash(const int *d_J, int B_thresh, const int *d_J2, int 
     return GSFFT_ERR_UNSUPPORTED;
   cudaStream_t st = S(stream);
   const int words = W_RLFC / 32;
-  unsigned *bm = nullptr;
+  unsigned *bm = nullptr, *d_ep = nullptr;
   int *cnt = nullptr, *blk = nullptr;
   RunCtl *ctl = nullptr;
   int s = GSFFT_OK;
   if (cudaMalloc(&bm, sizeof(unsigned) * words) != cudaSuccess ||
       cudaMalloc(&cnt, sizeof(int) * B_thresh) != cudaSuccess ||
       cudaMalloc(&blk, sizeof(int) * vote_block_ints(B_thresh)) != cudaSuccess ||
-      cudaMalloc(&ctl, sizeof(RunCtl)) != cudaSuccess)
+      cudaMalloc(&ctl, sizeof(RunCtl)) != cudaSuccess ||
+      cudaMalloc(&d_ep, sizeof(unsigned)) != cudaSuccess)
     s = GSFFT_ERR_ALLOC;
   Draws d;
   memset(&d, 0, sizeof(d));
@@ -410,11 +422,13 @@ int gsfft_stage_reverse_hash(const int *d_J, int B_thresh, const int *d_J2, int 
   memset(&c, 0, sizeof(c));
   c.cand_count = *h_count;
   c.num_rlfc = num_RLFC;
-  if (s == GSFFT_OK && cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st) != cudaSuccess)
+  if (s == GSFFT_OK && (cudaMemcpyAsync(ctl, &c, sizeof(c), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+                        cudaMemcpyAsync(d_ep, &epoch, sizeof(unsigned), cudaMemcpyHostToDevice, st) !=
+                            cudaSuccess))
     s = GSFFT_ERR_CUDA;
   if (s == GSFFT_OK) s = launch_sigma_bitmaps(d_J2, ctl, num_RLFC, W_RLFC, 1, d, bm, ctl, st);
   if (s == GSFFT_OK)
-    s = launch_vote_loop(0, d_J, B_thresh, n, B, W_RLFC, bm, d, loops_thresh, epoch, d_vote, d_cand,
+    s = launch_vote_loop(0, d_J, B_thresh, n, B, W_RLFC, bm, d, loops_thresh, d_ep, d_vote, d_cand,
                          cap, cnt, blk, ctl, true, st);
   if (s == GSFFT_OK && cudaMemcpyAsync(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost, st) != cudaSuccess)
     s = GSFFT_ERR_CUDA;
@@ -427,6 +441,7 @@ int gsfft_stage_reverse_hash(const int *d_J, int B_thresh, const int *d_J2, int 
   cudaFree(cnt);
   cudaFree(blk);
   cudaFree(ctl);
+  cudaFree(d_ep);
   return s;
 }
 

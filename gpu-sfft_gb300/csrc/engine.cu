@@ -31,6 +31,15 @@ __global__ void convert_taps_kernel(const double2 *__restrict__ src, void *dst, 
   else reinterpret_cast<double2 *>(dst)[i] = v;
 }
 
+// First kernel of every run: clears the run state and the row maxima and
+// advances the device epoch (a graph replay of the run advances it too).
+__global__ void run_begin_kernel(RunCtl *ctl, unsigned long long *rmax, int nrmax, unsigned *epoch) {
+  int *c = reinterpret_cast<int *>(ctl);
+  for (int i = threadIdx.x; i < (int)(sizeof(RunCtl) / sizeof(int)); i += blockDim.x) c[i] = 0;
+  for (int i = threadIdx.x; i < nrmax; i += blockDim.x) rmax[i] = 0ull;
+  if (threadIdx.x == 0) *epoch = *epoch + 1u;
+}
+
 // hinv[idx] = conj(H)/|H|^2 with H = filter_freq[(n - d) mod n], d = idx - nb/2
 __global__ void hinv_kernel(const double2 *__restrict__ ff, int n, int nb, double2 *hinv) {
   const int idx = blockIdx.x * 256 + threadIdx.x;
@@ -107,6 +116,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   A(topk_idx, sizeof(int) * (size_t)p.k + 16);
   A(topk, sizeof(DevNode) * (size_t)p.k + 16);
   A(ctl, sizeof(RunCtl));
+  A(d_epoch, sizeof(unsigned) * 4);
   A(rmax, sizeof(unsigned long long) * (size_t)(p.RLFC_loops + p.loops));
   // perm+filter form: one ordered pass over x when that moves fewer DRAM bytes
   // than loops*w + RLFC_loops*W random reads (~80 bytes per random read)
@@ -135,6 +145,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   if (s == GSFFT_OK) {
     cudaError_t e = cudaMemset(P->vote, 0, sizeof(unsigned) * (size_t)p.n);
     if (e == cudaSuccess) e = cudaMemset(P->ctl, 0, sizeof(RunCtl));
+    if (e == cudaSuccess) e = cudaMemset(P->d_epoch, 0, sizeof(unsigned) * 4);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
       set_last_error("plan init: %s", cudaGetErrorString(e));
@@ -155,7 +166,7 @@ void plan_destroy(Plan *P) {
   void *ptrs[] = {P->filt, P->hinv, P->rsamp, P->J2b, P->J2, P->bins, P->bsamp, P->J,
                   P->bm_j2, P->bm_sig, P->tile_tmp, P->vote, P->cand, P->cnt, P->blk,
                   P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax, P->ybuf, P->bpart,
-                  P->filt_bm};
+                  P->filt_bm, P->d_epoch};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
@@ -190,8 +201,19 @@ int plan_set_filter(Plan *P, const void *d_ft, const void *d_ff, cudaStream_t st
   return GSFFT_OK;
 }
 
+int plan_epoch_advance(Plan *P, cudaStream_t st) {
+  // epoch-tagged vote table: cleared only when the 24-bit epoch would wrap
+  if (P->epoch + 1u >= (1u << 24)) {
+    GS_CUDA(cudaMemsetAsync(P->vote, 0, sizeof(unsigned) * (size_t)P->p.n, st));
+    GS_CUDA(cudaMemsetAsync(P->d_epoch, 0, sizeof(unsigned), st));
+    P->epoch = 0;
+  }
+  P->epoch++;  // the run's first kernel makes the same step on the device
+  return GSFFT_OK;
+}
+
 int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int *ai,
-             cudaStream_t st) {
+             cudaStream_t st, bool capturing) {
   if (!P->filter_set) return GSFFT_ERR_STATE;
   const gsfft_params &p = P->p;
   const int before = g_launch_counter;
@@ -208,19 +230,15 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
     d.a[l] = a[l];
     d.ai[l] = ai[l];
   }
-  // epoch-tagged vote table: clear only when the 24-bit epoch wraps
-  P->epoch++;
-  if (P->epoch >= (1u << 24)) {
-    GS_CUDA(cudaMemsetAsync(P->vote, 0, sizeof(unsigned) * (size_t)p.n, st));
-    P->epoch = 1;
-  }
-  GS_CUDA(cudaMemsetAsync(P->ctl, 0, sizeof(RunCtl), st));
+  if (!capturing) GS_CHECK(plan_epoch_advance(P, st));
   const int kb = P->precision == GSFFT_FP64 ? 8 : 4;
-  GS_CUDA(cudaMemsetAsync(P->rmax, 0, sizeof(unsigned long long) * (p.RLFC_loops + p.loops), st));
+  run_begin_kernel<<<1, 64, 0, st>>>(P->ctl, (unsigned long long *)P->rmax, p.RLFC_loops + p.loops,
+                                     P->d_epoch);
+  GS_LAUNCHED();
   void *rmax_w = P->rmax;  // RLFC rows, then bucket rows (u64 in FP64, u32 in FP32)
   void *rmax_b = (char *)P->rmax + (size_t)kb * p.RLFC_loops;
   cudaEvent_t *ev = nullptr;
-  if (P->timing && P->timed_runs < 512) {
+  if (P->timing && !capturing && P->timed_runs < 512) {
     const size_t need = (size_t)(P->timed_runs + 1) * (2 * ST_COUNT);
     while (P->events.size() < need) {
       cudaEvent_t e;
@@ -300,7 +318,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   const size_t wW = (size_t)p.W_RLFC / 32;
   for (int l = 0; l < p.loops_loc; l++)
     GS_CHECK(launch_vote_loop(l, P->J + (size_t)l * p.B_thresh, p.B_thresh, p.n, p.B, p.W_RLFC,
-                              P->bm_sig + wW * l, d, p.loops_thresh, P->epoch, P->vote, P->cand,
+                              P->bm_sig + wW * l, d, p.loops_thresh, P->d_epoch, P->vote, P->cand,
                               P->cap, P->cnt, P->blk, P->ctl, l + 1 >= p.loops_thresh, st));
   END(ST_VOTE);
   // A8: estimation; A9: k largest

@@ -19,7 +19,8 @@ struct Plan {
   size_t es = 16;
   bool filter_set = false;
   bool ran = false;
-  unsigned epoch = 0;
+  unsigned epoch = 0;            // host mirror of *d_epoch after the last queued run
+  unsigned *d_epoch = nullptr;   // device copy, advanced by each run's first kernel
   int launches_per_run = 0;
   FftPlan fftB, fftW;
   SelectScratch selB, selW, selK;
@@ -56,8 +57,13 @@ int plan_create(const gsfft_params &p, int precision, unsigned flags, int max_ca
 void plan_destroy(Plan *P);
 int plan_set_filter(Plan *P, const void *d_filter_time, const void *d_filter_freq,
                     cudaStream_t st);
+// capturing = true while a CUDA graph records the run: the host-side epoch
+// bookkeeping and stage timing are then left to whoever launches the graph.
 int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int *ai,
-             cudaStream_t st);
+             cudaStream_t st, bool capturing = false);
+// host side of a run's epoch step (clears the vote table when the 24-bit
+// epoch would wrap); called once per queued run, before the run's kernels
+int plan_epoch_advance(Plan *P, cudaStream_t st);
 int plan_results(Plan *P, Node *h_nodes, int nodes_cap, int *I_F, Node *h_topk, int topk_cap,
                  int *n_topk, cudaStream_t st);
 int plan_enable_timing(Plan *P, bool on);
@@ -72,7 +78,9 @@ int launch_convert_taps(const double2 *d_ft, void *dst, int w, bool to_float, cu
 struct Batch;
 int batch_create(Plan *const *plans, int count, int nstreams, Batch **out);
 int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, const int *ai,
-              cudaStream_t st);
+              cudaStream_t st, bool capturing = false);
+int batch_capture(Batch *b, const void *const *d_x, const int *offs, const int *a, const int *ai);
+int batch_launch(Batch *b, cudaStream_t st);
 void batch_destroy(Batch *b);
 
 // signal ingest and device-side evaluation (host_io.cu)

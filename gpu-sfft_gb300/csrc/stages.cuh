@@ -68,10 +68,11 @@ int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, co
                              unsigned *bitmaps, RunCtl *ctl, cudaStream_t st);
 
 // A7: one location loop of voting; appends candidates in canonical order.
+// epoch: device word with the run's epoch (vote entries are epoch << 8 | count).
 // may_complete = false (location loop l < loops_thresh - 1 of a run, where no
 // count can reach the threshold) only records the votes.
 int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
-                     const unsigned *bitmap_l, const Draws &d, int loops_thresh, unsigned epoch,
+                     const unsigned *bitmap_l, const Draws &d, int loops_thresh, const unsigned *epoch,
                      unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
                      bool may_complete, cudaStream_t st);
 // ints needed by the blk scratch of launch_vote_loop

@@ -228,8 +228,9 @@ __device__ __forceinline__ unsigned warp_excl_scan(unsigned v, unsigned *total) 
 constexpr int WPB = VT / 32;  // buckets (warps) per block
 
 __global__ void __launch_bounds__(VT)
-vote_count_kernel(WalkArgs w, unsigned epoch, unsigned thresh, unsigned *vote, int *cnt, int *blk,
-                  int *blk_pre, RunCtl *ctl) {
+vote_count_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, unsigned *vote, int *cnt,
+                  int *blk, int *blk_pre, RunCtl *ctl) {
+  const unsigned epoch = *epoch_p;
   __shared__ unsigned ws[VT / 32];
   __shared__ int is_last;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -299,7 +300,8 @@ vote_count_kernel(WalkArgs w, unsigned epoch, unsigned thresh, unsigned *vote, i
 // Location loops before the (loops_thresh-1)-th cannot bring any count to
 // the threshold: they only record their votes.
 __global__ void __launch_bounds__(VT)
-vote_mark_kernel(WalkArgs w, unsigned epoch, unsigned *vote) {
+vote_mark_kernel(WalkArgs w, const unsigned *epoch_p, unsigned *vote) {
+  const unsigned epoch = *epoch_p;
   const int warp = threadIdx.x >> 5;
   const int t = blockIdx.x * WPB + warp;
   if (t >= w.Bt) return;
@@ -331,7 +333,7 @@ vote_mark_kernel(WalkArgs w, unsigned epoch, unsigned *vote) {
 }
 
 __global__ void __launch_bounds__(VT)
-vote_write_kernel(WalkArgs w, unsigned epoch, unsigned thresh, const unsigned *__restrict__ vote,
+vote_write_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, const unsigned *__restrict__ vote,
                   const int *__restrict__ cnt, const int *__restrict__ blk_pre, int nblk, int *cand,
                   int cap, RunCtl *ctl) {
   __shared__ unsigned ws[VT / 32];
@@ -346,7 +348,7 @@ vote_write_kernel(WalkArgs w, unsigned epoch, unsigned thresh, const unsigned *_
   const unsigned cw = __shfl_sync(0xffffffffu, c, 0);
   if (cw) {
     const unsigned nmask = (unsigned)w.n - 1u;
-    const unsigned want = (epoch << 8) | thresh;
+    const unsigned want = (*epoch_p << 8) | thresh;
     for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
       // appended positions of this lane, in bit order
       unsigned app = 0;
@@ -433,7 +435,7 @@ int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, co
 }
 
 int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
-                     const unsigned *bitmap_l, const Draws &d, int loops_thresh, unsigned epoch,
+                     const unsigned *bitmap_l, const Draws &d, int loops_thresh, const unsigned *epoch,
                      unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
                      bool may_complete, cudaStream_t st) {
   WalkArgs w;

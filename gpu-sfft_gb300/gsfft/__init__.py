@@ -86,6 +86,8 @@ def lib():
         "gsfft_batch_create": ([C.POINTER(P), i, i, C.POINTER(P)], i),
         "gsfft_batch_destroy": ([P], i),
         "gsfft_run_batched": ([P, C.POINTER(P), P, P, P, P], i),
+        "gsfft_batch_capture": ([P, C.POINTER(P), P, P, P], i),
+        "gsfft_batch_launch": ([P, P], i),
         "gsfft_alloc": ([C.POINTER(P), C.c_size_t], i),
         "gsfft_free": ([P], i),
         "gsfft_copy": ([P, P, C.c_size_t, P], i),
@@ -181,8 +183,7 @@ class Batch:
         check(lib().gsfft_batch_create(arr, len(self.plans), streams, C.byref(h)), "gsfft_batch_create")
         self.h = h
 
-    def run(self, d_xs, draws, stream=0):
-        """d_xs: device pointers, draws: per plan (offsets, a, ai)."""
+    def _pack(self, d_xs, draws):
         n = len(self.plans)
         offs = np.zeros((n, MAX_RLFC_LOOPS), np.int32)
         a = np.zeros((n, MAX_LOOPS), np.int32)
@@ -192,8 +193,22 @@ class Batch:
             a[i, :len(aa)] = aa
             ai[i, :len(ii)] = ii
         xs = (C.c_void_p * n)(*[int(v) for v in d_xs])
+        return xs, offs, a, ai
+
+    def run(self, d_xs, draws, stream=0):
+        """d_xs: device pointers, draws: per plan (offsets, a, ai)."""
+        xs, offs, a, ai = self._pack(d_xs, draws)
         check(lib().gsfft_run_batched(self.h, xs, _np_ptr(offs), _np_ptr(a), _np_ptr(ai),
                                       stream or None), "gsfft_run_batched")
+
+    def capture(self, d_xs, draws):
+        """Record one batched run into a CUDA graph (replayed by launch())."""
+        xs, offs, a, ai = self._pack(d_xs, draws)
+        check(lib().gsfft_batch_capture(self.h, xs, _np_ptr(offs), _np_ptr(a), _np_ptr(ai)),
+              "gsfft_batch_capture")
+
+    def launch(self, stream=0):
+        check(lib().gsfft_batch_launch(self.h, stream or None), "gsfft_batch_launch")
 
     def close(self):
         if self.h:

@@ -169,6 +169,18 @@ int gsfft_batch_destroy(gsfft_batch batch);
 int gsfft_run_batched(gsfft_batch batch, const void *const *d_x, const int *h_rlfc_offsets,
                       const int *h_a, const int *h_ai, void *stream);
 
+/* Graph form of gsfft_run_batched: gsfft_batch_capture records one batched
+ * run with these signal buffers and draws into a CUDA graph (nothing runs);
+ * every gsfft_batch_launch then replays the whole batch with one graph launch
+ * on stream, transforming whatever the captured d_x buffers hold at that
+ * time, with the captured draws.  Results are read per plan as usual after a
+ * launch.  Capturing again replaces the graph.  Returns GSFFT_ERR_STATE when
+ * launched before a capture, GSFFT_ERR_UNSUPPORTED when the CUDA graph
+ * cannot be built (the error text says why). */
+int gsfft_batch_capture(gsfft_batch batch, const void *const *d_x, const int *h_rlfc_offsets,
+                        const int *h_a, const int *h_ai);
+int gsfft_batch_launch(gsfft_batch batch, void *stream);
+
 /* ---- host I/O and evaluation ---------------------------------------- */
 
 /* Device memory and copies for callers that do not link the CUDA runtime

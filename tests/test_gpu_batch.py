@@ -50,3 +50,33 @@ def test_batched_equals_single(G, torch_cuda, streams):
     batch.close()
     for it in items:
         it[0].close()
+
+
+def test_batch_graph_replays(G, torch_cuda):
+    """A captured batch replays with one graph launch: on new signal contents
+    written into the captured buffers, and twice in a row (each replay must
+    count votes afresh), it gives exactly the single-plan results."""
+    torch = torch_cuda
+    items = [_setup(G, torch, cfg, prec, 200 + i) for i, (cfg, prec) in enumerate(CASES)]
+    batch = G.Batch([it[0] for it in items], streams=4)
+    batch.capture([it[1].data_ptr() for it in items], [it[2] for it in items])
+    stream = torch.cuda.Stream()
+    for rep in range(2):
+        # new signal contents in the captured buffers
+        for i, (plan, d_x, draws, _) in enumerate(items):
+            p = plan.params
+            x, _, _, _ = synth.signal_numpy(p.n, p.k, seed=300 + 10 * rep + i)
+            d_x.copy_(torch.from_numpy(x.astype(np.complex128 if plan.precision == 0 else np.complex64)))
+        torch.cuda.synchronize()
+        batch.launch(stream=stream.cuda_stream)
+        stream.synchronize()
+        got = [plan.results() for plan, _, _, _ in items]
+        for (plan, d_x, draws, _), g in zip(items, got):
+            plan.run(d_x.data_ptr(), *draws)
+            ref = plan.results()
+            assert g["I_F"] == ref["I_F"]
+            np.testing.assert_array_equal(g["nodes"], ref["nodes"])
+            np.testing.assert_array_equal(g["topk"], ref["topk"])
+    batch.close()
+    for it in items:
+        it[0].close()
