@@ -218,9 +218,31 @@ int gsfft_batch_launch(gsfft_batch batch, void *stream) {
   return batch_launch(batch->impl, S(stream));
 }
 
-/* ---------------------------------------------------------------- host I/O */
+/* ---------------------------------------------------------------- tensor cores */
 
 static int sync_check(cudaStream_t st, const char *what);
+
+int gsfft_tc_dft64(const void *d_in, void *d_out, int nvec, void *stream) {
+  if (!d_in || !d_out || nvec < 0) return GSFFT_ERR_PARAM;
+  if (nvec == 0) return GSFFT_OK;
+  int *err = nullptr;
+  if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return GSFFT_ERR_ALLOC;
+  int s = cudaMemsetAsync(err, 0, sizeof(int), S(stream)) == cudaSuccess ? GSFFT_OK : GSFFT_ERR_CUDA;
+  if (s == GSFFT_OK) s = launch_tc_dft64(d_in, d_out, nvec, err, S(stream));
+  if (s == GSFFT_OK) s = sync_check(S(stream), "gsfft_tc_dft64");
+  int herr = 0;
+  if (s == GSFFT_OK && cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    s = GSFFT_ERR_CUDA;
+  if (s == GSFFT_OK && herr) {
+    set_last_error("gsfft_tc_dft64: a tensor-core completion wait timed out");
+    s = GSFFT_ERR_CUDA;
+  }
+  cudaFree(err);
+  return s;
+}
+
+/* ---------------------------------------------------------------- host I/O */
+
 
 int gsfft_alloc(void **d_ptr, size_t bytes) {
   if (!d_ptr) return GSFFT_ERR_PARAM;

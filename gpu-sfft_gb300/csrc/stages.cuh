@@ -83,6 +83,10 @@ int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, 
                     int loops, int n, int B, const Draws &d, const double2 *hinv,
                     DevNode *nodes, double *mag2, cudaStream_t st);
 
+// 64-point complex DFTs of nvec float2 vectors on the tensor cores (tcgen05,
+// three-part bf16 split, fp32 accumulation); err: set when a wait timed out
+int launch_tc_dft64(const void *x, void *y, int nvec, int *err, cudaStream_t st);
+
 // gather selected nodes (A9 output)
 int launch_gather_nodes(const DevNode *nodes, const int *idx, const int *count, int cap,
                         DevNode *out, cudaStream_t st);

@@ -88,6 +88,7 @@ def lib():
         "gsfft_run_batched": ([P, C.POINTER(P), P, P, P, P], i),
         "gsfft_batch_capture": ([P, C.POINTER(P), P, P, P], i),
         "gsfft_batch_launch": ([P, P], i),
+        "gsfft_tc_dft64": ([P, P, i, P], i),
         "gsfft_alloc": ([C.POINTER(P), C.c_size_t], i),
         "gsfft_free": ([P], i),
         "gsfft_copy": ([P, P, C.c_size_t, P], i),
@@ -220,6 +221,11 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def tc_dft64(d_in, d_out, nvec, stream=0):
+    """nvec forward 64-point DFTs of complex64 vectors on the tensor cores."""
+    check(lib().gsfft_tc_dft64(d_in, d_out, nvec, stream or None), "gsfft_tc_dft64")
 
 
 def ingest(h_x, precision, d_x, stream=0):

@@ -220,6 +220,13 @@ int gsfft_evaluate(gsfft_plan plan, const complex_t *d_x_f, const int *d_true_lo
 int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
               int precision, void *stream);
 
+/* Tensor-core building block of the mixed bucket FFT (the DFT stages that
+ * replace cuFFT's B-point transform, innerLoop.cu:247-262): nvec independent
+ * forward 64-point DFTs of {float, float} vectors (d_in, d_out: nvec * 64
+ * elements), computed with tcgen05 matrix products of three-part bf16 splits
+ * accumulated in fp32 (FP32-level accuracy). */
+int gsfft_tc_dft64(const void *d_in, void *d_out, int nvec, void *stream);
+
 /* Cutoff (innerLoop.cu:551-616): indices of the num largest samples, ascending;
  * ties at the threshold resolved in ascending index order.  batch independent
  * rows of `size` samples each (double or float per precision). */
