@@ -257,7 +257,9 @@ def run_ours(args, cfg):
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
     pf_flag = {"auto": 0, "gather": gsfft.FLAG_FORCE_GATHER, "stream": gsfft.FLAG_FORCE_STREAM}[args.pf]
-    plans = {"fp64": gsfft.Plan(p, gsfft.FP64, pf_flag), "mixed": gsfft.Plan(p, gsfft.MIXED, pf_flag)}
+    tc_flag = gsfft.FLAG_TC_BUCKET_FFT if args.tc_bucket else 0
+    plans = {"fp64": gsfft.Plan(p, gsfft.FP64, pf_flag),
+             "mixed": gsfft.Plan(p, gsfft.MIXED, pf_flag | tc_flag)}
     for pl in plans.values():
         pl.set_filter(d_ft.data_ptr(), d_ff.data_ptr(), sh)
     xin = {"fp64": x64, "mixed": x32}
@@ -613,6 +615,11 @@ def main():
                     help="small: n=2^25, k=4000 (same W_RLFC) for profiler captures")
     ap.add_argument("--pf", default="auto", choices=["auto", "gather", "stream"],
                     help="perm+filter form (auto: by the plan's DRAM byte model)")
+    ap.add_argument("--tc-bucket", dest="tc_bucket", action="store_true",
+                    help="mixed bucket FFT with tensor-core passes")
+    ap.add_argument("--cc-bucket", dest="tc_bucket", action="store_false",
+                    help="mixed bucket FFT on CUDA cores only")
+    ap.set_defaults(tc_bucket=False)
     ap.add_argument("--only-mixed", action="store_true",
                     help="time only the mixed path and print its stage times (profiling runs)")
     args = ap.parse_args()

@@ -137,7 +137,13 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   }
 #undef A
   P->floor_rel = (flags & GSFFT_FLAG_RAW_SELECTION) ? 0.0 : 1e-10;
-  if (s == GSFFT_OK) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
+  if (s == GSFFT_OK) {
+    int t = GSFFT_ERR_UNSUPPORTED;
+    if (precision == GSFFT_MIXED && (flags & GSFFT_FLAG_TC_BUCKET_FFT))
+      t = fft_plan_init_tc(P->fftB, p.B, p.loops);
+    P->tc_bucket = t == GSFFT_OK;
+    if (!P->tc_bucket) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
+  }
   if (s == GSFFT_OK) s = fft_plan_init(P->fftW, p.W_RLFC, precision, p.RLFC_loops);
   if (s == GSFFT_OK) s = select_scratch_init(P->selB, p.loops_loc, p.B);
   if (s == GSFFT_OK) s = select_scratch_init(P->selW, p.RLFC_loops, p.W_RLFC);
@@ -299,6 +305,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
     FftIo io;
     io.samples = P->bsamp;
     io.row_max = rmax_b;
+    io.err = &P->ctl->err;
     const void *src = P->bins;
     if (P->use_stream) {  // the row-group partials are added by the first pass
       src = P->bpart;

@@ -44,6 +44,7 @@ struct Plan {
   void *filt_bm = nullptr; // bucket-major taps of the streaming perm+filter
   int groups = 1;
   bool use_stream = false;
+  bool tc_bucket = false;  // bucket FFT with tensor-core passes
   double floor_rel = 1e-10;
   // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
   bool timing = false;

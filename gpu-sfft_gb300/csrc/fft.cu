@@ -418,6 +418,8 @@ int launch_pass(const PassArgs &a, long long total_sub, cudaStream_t st) {
 template <typename T>
 int dispatch_pass(int logr, const PassArgs &a, long long total_sub, cudaStream_t st) {
   switch (logr) {
+    case 5: return launch_pass<T, 5>(a, total_sub, st);
+    case 6: return launch_pass<T, 6>(a, total_sub, st);
     case 7: return launch_pass<T, 7>(a, total_sub, st);
     case 8: return launch_pass<T, 8>(a, total_sub, st);
     case 9: return launch_pass<T, 9>(a, total_sub, st);
@@ -490,6 +492,43 @@ int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch) {
   return GSFFT_OK;
 }
 
+// FP32 plan whose last two passes are radix-64 tensor-core passes: n = 2^L
+// with a CUDA-core first pass of radix 2^(L-12) (5 <= L-12 <= 14).
+int fft_plan_init_tc(FftPlan &p, long long n, int max_batch) {
+  fft_plan_free(p);
+  if (n < 256 || (n & (n - 1)) != 0) return GSFFT_ERR_UNSUPPORTED;
+  int L = 0;
+  while ((1LL << L) < n) L++;
+  if (L - 12 < 5 || L - 12 > 14) return GSFFT_ERR_UNSUPPORTED;
+  p.n = n;
+  p.L = L;
+  p.precision = GSFFT_MIXED;
+  p.npass = 3;
+  p.logR[0] = L - 12;
+  p.logR[1] = 6;
+  p.logR[2] = 6;
+  p.tc[0] = false;
+  p.tc[1] = p.tc[2] = true;
+  long long Np = 1;
+  for (int i = 0; i < p.npass; i++) {
+    const long long R = 1LL << p.logR[i];
+    Np *= R;
+    int lg = 0;
+    while ((1LL << lg) < Np) lg++;
+    const int h = (lg + 1) / 2;
+    p.tw_h[i] = h;
+    const long long nlo = 1LL << h, nhi = (Np + nlo - 1) / nlo;
+    GS_CHECK(make_table<float>(&p.tw_lo[i], nlo, 1, Np));
+    GS_CHECK(make_table<float>(&p.tw_hi[i], nhi, nlo, Np));
+    GS_CHECK(make_table<float>(&p.tw_R[i], R, 1, R));
+  }
+  GS_CHECK(tc_build_F(&p.tc_F));
+  p.scratch_elems = (long long)n * max_batch * 2;
+  GS_CUDA(cudaMalloc(&p.scratch, sizeof(float2) * p.scratch_elems));
+  GS_CUDA(cudaDeviceSynchronize());
+  return GSFFT_OK;
+}
+
 void fft_plan_free(FftPlan &p) {
   for (int i = 0; i < 3; i++) {
     if (p.tw_hi[i]) cudaFree(p.tw_hi[i]);
@@ -499,6 +538,9 @@ void fft_plan_free(FftPlan &p) {
   }
   if (p.scratch) cudaFree(p.scratch);
   p.scratch = nullptr;
+  if (p.tc_F) cudaFree(p.tc_F);
+  p.tc_F = nullptr;
+  for (int i = 0; i < 3; i++) p.tc[i] = false;
   p.npass = 0;
 }
 
@@ -548,8 +590,30 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
     a.write_complex = last ? (io.write_complex ? 1 : 0) : 1;
     const long long total_sub = (p.n >> p.logR[i]) * batch;
     a.total = total_sub;
-    int s = dbl ? dispatch_pass<double>(p.logR[i], a, total_sub, st)
-                : dispatch_pass<float>(p.logR[i], a, total_sub, st);
+    int s;
+    if (p.tc[i]) {
+      if (i == 0 || dbl) return GSFFT_ERR_UNSUPPORTED;  // no gather / partial loader here
+      TcPassArgs t;
+      t.in = a.in;
+      t.out = a.out;
+      t.logN = a.logN;
+      t.logNs = a.logNs;
+      t.bstride = a.bstride;
+      t.total = total_sub;
+      t.inverse = a.inverse;
+      t.tw_hi = a.tw_hi;
+      t.tw_lo = a.tw_lo;
+      t.tw_h = a.tw_h;
+      t.F = p.tc_F;
+      t.samples = a.samples;
+      t.row_max = a.row_max;
+      t.write_complex = a.write_complex;
+      t.err = io.err;
+      s = launch_tc_pass(t, st);
+    } else {
+      s = dbl ? dispatch_pass<double>(p.logR[i], a, total_sub, st)
+              : dispatch_pass<float>(p.logR[i], a, total_sub, st);
+    }
     if (s != GSFFT_OK) return s;
     src = dst;
     Ns <<= p.logR[i];

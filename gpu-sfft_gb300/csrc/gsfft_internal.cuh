@@ -78,9 +78,29 @@ struct FftPlan {
   void *tw_lo[3] = {nullptr, nullptr, nullptr};
   int tw_h[3] = {0, 0, 0};
   void *tw_R[3] = {nullptr, nullptr, nullptr};  // exp(-2 pi i m / R) for the pass radix
+  bool tc[3] = {false, false, false};  // pass runs on the tensor cores (radix 64, FP32)
+  void *tc_F = nullptr;                // DFT_64 operand of the tensor-core passes
   void *scratch = nullptr; // one transform-sized buffer per batch entry (multi-pass)
   long long scratch_elems = 0;
 };
+
+// One radix-64 pass of an FP32 FFT on the tensor cores (tc_dft.cu).
+struct TcPassArgs {
+  const void *in;       // float2
+  void *out;            // float2
+  int logN, logNs;
+  long long bstride, total;  // row stride; sub-transforms over the batch
+  int inverse;
+  const void *tw_hi, *tw_lo;
+  int tw_h;
+  const void *F;        // three bf16 parts of the DFT_64 real form (tc_build_F)
+  void *samples;        // float |X|^2 or null
+  void *row_max;        // u32 bit pattern per row, with samples
+  int write_complex;
+  int *err;             // set when a completion wait timed out (may be null)
+};
+int tc_build_F(void **F);
+int launch_tc_pass(const TcPassArgs &a, cudaStream_t st);
 
 // Optional fused prologue/epilogue of an FFT execution.
 struct FftIo {
@@ -98,9 +118,14 @@ struct FftIo {
   // u32 for float) accumulated with atomicMax; the caller zeroes it first
   void *row_max = nullptr;
   bool write_complex = true;
+  // tensor-core passes: set when a completion wait timed out (may be null)
+  int *err = nullptr;
 };
 
 int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch);
+// FP32 plan with radix-64 tensor-core passes (last two); GSFFT_ERR_UNSUPPORTED
+// when n does not decompose as 2^(5..14) x 64 x 64
+int fft_plan_init_tc(FftPlan &p, long long n, int max_batch);
 void fft_plan_free(FftPlan &p);
 // in: batch entries at in + b*n; out: out + b*n.  sign -1 forward, +1 inverse.
 int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,

@@ -198,6 +198,256 @@ tc_dft64_kernel(const float2 *__restrict__ x, float2 *__restrict__ y, int nvec, 
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N) : "memory");
 }
 
+// The three bf16 parts of F (real form of DFT_64) in the K-major layout,
+// 3 x 32 KiB, built once per FFT plan.
+__global__ void tc_build_F_kernel(unsigned char *F) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= TC_M * TC_K) return;
+  const int m = e / TC_K, k = e % TC_K;
+  const int o = m & 63, i = k & 63;
+  double s, c;
+  sincospi(-2.0 * (double)((o * i) & 63) / 64.0, &s, &c);
+  float f;
+  if (m < 64) f = (k < 64) ? (float)c : (float)(-s);
+  else f = (k < 64) ? (float)s : (float)c;
+  __nv_bfloat16 p0, p1, p2;
+  split3(f, p0, p1, p2);
+  const int off = kmajor_off(m, k, TC_K);
+  *reinterpret_cast<__nv_bfloat16 *>(F + off) = p0;
+  *reinterpret_cast<__nv_bfloat16 *>(F + A_BYTES + off) = p1;
+  *reinterpret_cast<__nv_bfloat16 *>(F + 2 * A_BYTES + off) = p2;
+}
+
+constexpr int TP_THREADS = 256;  // two warpgroups: TMEM quadrant = warp % 4
+constexpr int DP = 68;           // row pitch (floats) of the fp32 result staged in shared memory
+static_assert(128 * DP * 4 <= 3 * B_BYTES, "result staging fits the X parts");
+
+__device__ __forceinline__ unsigned pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return (unsigned)__bfloat16_as_ushort(lo) | ((unsigned)__bfloat16_as_ushort(hi) << 16);
+}
+
+// One radix-64 Stockham pass of an FP32 FFT (the index scheme of
+// fft_pass_kernel): sub-transform u of batch row b = u / S takes
+// v[r] = in[j + r S] * w((j mod Ns) r / (Ns 64)), V = DFT_64(v),
+// out[(j / Ns) Ns 64 + (j mod Ns) + k Ns] = V[k].  64 sub-transforms per
+// tile; persistent CTAs.  F arrives by one bulk copy overlapping the first
+// tile's loads.
+__global__ void __launch_bounds__(TP_THREADS, 1) tc_pass_kernel(TcPassArgs a) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  unsigned char *A = tsm;
+  unsigned char *Bm = tsm + 3 * A_BYTES;               // X parts; reused as the fp32 result
+  float *D = reinterpret_cast<float *>(Bm);            // [128][DP]
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tsm + 3 * A_BYTES + 3 * B_BYTES);
+  unsigned long long *fbar = bar + 1;                  // F arrival
+  unsigned *tmem_slot = reinterpret_cast<unsigned *>(bar + 2);
+  unsigned *red = tmem_slot + 1;                       // [8] warp maxima
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float2 *__restrict__ in = reinterpret_cast<const float2 *>(a.in);
+  float2 *__restrict__ out = reinterpret_cast<float2 *>(a.out);
+  float *__restrict__ smp = reinterpret_cast<float *>(a.samples);
+  const float2 *__restrict__ thi = reinterpret_cast<const float2 *>(a.tw_hi);
+  const float2 *__restrict__ tlo = reinterpret_cast<const float2 *>(a.tw_lo);
+  const int logS = a.logN - 6;
+  const long long Smask = (1LL << logS) - 1;
+  const int logNs = a.logNs;
+  const long long Nsmask = (1LL << logNs) - 1;
+  const int hmask = (1 << a.tw_h) - 1;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(TC_N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(fbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // F: one 96 KiB bulk copy, completion counted on fbar
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(fbar)),
+                 "r"(3 * A_BYTES)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(A)),
+        "l"(a.F), "r"(3 * A_BYTES), "r"(smem_addr(fbar))
+        : "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = *tmem_slot;
+  constexpr unsigned IDESC = idesc_bf16(TC_M, TC_N);
+  unsigned phase = 0;
+  bool ok = true, f_ready = false;
+  const long long tiles = (a.total + TC_N - 1) / TC_N;
+
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long u0 = tile * TC_N;
+    // ---- load: two items (v, eight consecutive r) per thread, all 16 loads in flight
+    float2 xv[2][8];
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+      const int item = tid + it * TP_THREADS;
+      const int v = item & 63, r0 = (item >> 6) * 8;
+      const long long u = u0 + v;
+      const bool live = u < a.total;
+      const long long b = live ? (u >> logS) : 0, j = live ? (u & Smask) : 0;
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        xv[it][q] = live ? in[b * a.bstride + j + ((long long)(r0 + q) << logS)] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+      const int item = tid + it * TP_THREADS;
+      const int v = item & 63, r0 = (item >> 6) * 8;
+      const long long u = u0 + v;
+      const long long j = u & Smask;
+      unsigned wr[3][4], wi[3][4];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float2 x = xv[it][q];
+        if (a.inverse) x.y = -x.y;
+        if (logNs > 0) {
+          const long long mm = (j & Nsmask) * (r0 + q);
+          x = cmul(x, cmul(thi[mm >> a.tw_h], tlo[mm & hmask]));
+        }
+        __nv_bfloat16 r[3], im[3];
+        split3(x.x, r[0], r[1], r[2]);
+        split3(x.y, im[0], im[1], im[2]);
+        if (q & 1) {
+#pragma unroll
+          for (int pp = 0; pp < 3; pp++) {
+            wr[pp][q >> 1] |= (unsigned)__bfloat16_as_ushort(r[pp]) << 16;
+            wi[pp][q >> 1] |= (unsigned)__bfloat16_as_ushort(im[pp]) << 16;
+          }
+        } else {
+#pragma unroll
+          for (int pp = 0; pp < 3; pp++) {
+            wr[pp][q >> 1] = __bfloat16_as_ushort(r[pp]);
+            wi[pp][q >> 1] = __bfloat16_as_ushort(im[pp]);
+          }
+        }
+      }
+      const int offr = kmajor_off(v, r0, TC_K), offi = kmajor_off(v, 64 + r0, TC_K);
+#pragma unroll
+      for (int pp = 0; pp < 3; pp++) {
+        *reinterpret_cast<uint4 *>(Bm + pp * B_BYTES + offr) = make_uint4(wr[pp][0], wr[pp][1], wr[pp][2], wr[pp][3]);
+        *reinterpret_cast<uint4 *>(Bm + pp * B_BYTES + offi) = make_uint4(wi[pp][0], wi[pp][1], wi[pp][2], wi[pp][3]);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    // ---- six bf16 products into TMEM
+    if (tid == 0) {
+      bool go = true;
+      if (!f_ready) {
+        go = mbar_wait_bounded(smem_addr(fbar), 0);
+        f_ready = go;
+      }
+      if (go) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int pa[6] = {1, 0, 2, 0, 1, 0};
+        const int pb[6] = {1, 2, 0, 1, 0, 0};
+        for (int t = 0; t < 6; t++) {
+          const unsigned abase = smem_addr(A + pa[t] * A_BYTES);
+          const unsigned bbase = smem_addr(Bm + pb[t] * B_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < TC_K / 16; kk++) {
+            const unsigned long long ad = smem_desc(abase + kk * 256, 128, (TC_K / 8) * 128);
+            const unsigned long long bd = smem_desc(bbase + kk * 256, 128, (TC_K / 8) * 128);
+            const unsigned acc = (t > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                : "memory");
+          }
+        }
+      }
+      // the commit arrives even when nothing was issued, so the wait below ends
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_addr(bar))
+                   : "memory");
+      if (!go) {
+        ok = false;
+        if (a.err) atomicExch(a.err, 1);
+      }
+    }
+    if (!mbar_wait_bounded(smem_addr(bar), phase)) {
+      ok = false;
+      if (tid == 0 && a.err) atomicExch(a.err, 1);
+    }
+    ok = __syncthreads_and(ok) != 0;
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) break;
+    // ---- TMEM -> shared memory: warp w reads quadrant w % 4, columns 32 (w / 4) ..
+    {
+      const int q4 = warp & 3, h = warp >> 2;
+      const int m = 32 * q4 + lane;
+#pragma unroll
+      for (int c = 0; c < 32; c += 8) {
+        const int c0 = 32 * h + c;
+        unsigned r[8];
+        const unsigned taddr = tmem + ((unsigned)(32 * q4) << 16) + (unsigned)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        uint4 *d4 = reinterpret_cast<uint4 *>(D + m * DP + c0);
+        d4[0] = make_uint4(r[0], r[1], r[2], r[3]);
+        d4[1] = make_uint4(r[4], r[5], r[6], r[7]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    // ---- outputs: (v fast, k) pairs, complex and/or |X|^2
+    float tmax = 0.f;
+    const long long b_tile = u0 >> logS;  // S >= 64: the tile lies in one batch row
+#pragma unroll 4
+    for (int e = tid; e < TC_N * 64; e += TP_THREADS) {
+      const int v = e & 63, k = e >> 6;
+      const long long u = u0 + v;
+      if (u >= a.total) continue;
+      const long long j = u & Smask;
+      const float re = D[k * DP + v];
+      float im = D[(64 + k) * DP + v];
+      if (a.inverse) im = -im;
+      const long long dest = (u >> logS) * a.bstride + ((j >> logNs) << (logNs + 6)) + (j & Nsmask) +
+                             ((long long)k << logNs);
+      if (a.write_complex) out[dest] = make_float2(re, im);
+      if (smp) {
+        const float sq = __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+        smp[dest] = sq;
+        tmax = sq > tmax ? sq : tmax;
+      }
+    }
+    if (smp && a.row_max) {
+      unsigned kmax = __float_as_uint(tmax);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned y = __shfl_xor_sync(0xffffffffu, kmax, o);
+        kmax = y > kmax ? y : kmax;
+      }
+      if (lane == 0) red[warp] = kmax;
+      __syncthreads();
+      if (tid == 0) {
+        unsigned m8 = red[0];
+        for (int w2 = 1; w2 < TP_THREADS / 32; w2++) m8 = red[w2] > m8 ? red[w2] : m8;
+        atomicMax(reinterpret_cast<unsigned *>(a.row_max) + b_tile, m8);
+      }
+    }
+    __syncthreads();  // the result staging and X parts are rewritten by the next tile
+  }
+  // a CTA without tiles (or stopped early) still owns the F copy: wait for it
+  if (tid == 0 && !f_ready) (void)mbar_wait_bounded(smem_addr(fbar), 0);
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N) : "memory");
+}
+
 }  // namespace
 
 int launch_tc_dft64(const void *x, void *y, int nvec, int *err, cudaStream_t st) {
@@ -213,6 +463,31 @@ int launch_tc_dft64(const void *x, void *y, int nvec, int *err, cudaStream_t st)
   const int grid = tiles < sms ? tiles : sms;
   if (grid < 1) return GSFFT_OK;
   tc_dft64_kernel<<<grid, TC_THREADS, TC_SMEM, st>>>((const float2 *)x, (float2 *)y, nvec, err);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+int tc_build_F(void **F) {
+  GS_CUDA(cudaMalloc(F, 3 * A_BYTES));
+  tc_build_F_kernel<<<(TC_M * TC_K + 255) / 256, 256>>>(static_cast<unsigned char *>(*F));
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+int launch_tc_pass(const TcPassArgs &a, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    GS_CUDA(cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    attr = true;
+  }
+  if (a.logN - 6 < 6) return GSFFT_ERR_UNSUPPORTED;  // a tile of 64 must stay inside one row
+  int dev = 0, sms = 0;
+  GS_CUDA(cudaGetDevice(&dev));
+  GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const long long tiles = (a.total + TC_N - 1) / TC_N;
+  const int grid = (int)(tiles < sms ? tiles : sms);
+  if (grid < 1) return GSFFT_OK;
+  tc_pass_kernel<<<grid, TP_THREADS, TC_SMEM, st>>>(a);
   GS_LAUNCHED();
   return GSFFT_OK;
 }

@@ -24,6 +24,7 @@ FLAG_QUIRK_RESIDUE = 1
 FLAG_RAW_SELECTION = 2
 FLAG_FORCE_GATHER = 4
 FLAG_FORCE_STREAM = 8
+FLAG_TC_BUCKET_FFT = 16
 SELECTION_FLOOR = 1e-10
 OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE = range(7)
 

@@ -19,3 +19,44 @@ def test_tc_dft64_matches_numpy(G, torch_cuda, nvec):
     err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
     # three-part bf16 split with fp32 accumulation: FP32-level accuracy
     assert err.max() < 2e-6, err.max()
+
+
+def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
+    """Mixed engine with the tensor-core bucket FFT (B = 2^17 = 32 x 64 x 64)
+    against the CUDA-core mixed engine and the FP64 engine, same draws."""
+    from gsfft import synth
+    torch = torch_cuda
+    cfg = (24, 1600, 4.0, 2, 2, 5, 64, 2)
+    p, st = G.derive_params(*cfg)
+    assert st == 0 and p.B == 1 << 17
+    x, loc, coef, X = synth.signal_numpy(p.n, p.k, seed=5)
+    d_ft = torch.zeros(p.w, dtype=torch.complex128, device="cuda")
+    d_ff = torch.zeros(p.n, dtype=torch.complex128, device="cuda")
+    G.design_filter(p, d_ft.data_ptr(), d_ff.data_ptr())
+    d64 = torch.from_numpy(x).cuda()
+    d32 = d64.to(torch.complex64)
+    draws = synth.draws(5, p.n, p.W_RLFC, p.RLFC_loops, p.loops)
+    res = {}
+    for name, prec, flags, xx in [("fp64", G.FP64, 0, d64), ("mixed", G.MIXED, 0, d32),
+                                  ("tc", G.MIXED, G.FLAG_TC_BUCKET_FFT, d32)]:
+        plan = G.Plan(p, prec, flags)
+        plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+        plan.run(xx.data_ptr(), *draws)
+        r = plan.results()
+        assert r["status"] == 0
+        r["bins"] = plan.debug_stages()["bins"]
+        r["launches"] = plan.launches_per_run()
+        plan.close()
+        res[name] = r
+    assert res["tc"]["launches"] == res["mixed"]["launches"] + 1  # three bucket-FFT passes
+    b_tc = res["tc"]["bins"].astype(np.complex128)
+    b_cc = res["mixed"]["bins"].astype(np.complex128)
+    assert np.linalg.norm(b_tc - b_cc) / np.linalg.norm(b_cc) < 1e-5
+    k64 = res["fp64"]["topk"]["key"]
+    ktc = res["tc"]["topk"]["key"]
+    assert set(k64.tolist()) == set(ktc.tolist())
+    v64 = dict(zip(k64.tolist(), res["fp64"]["topk"]["x"] + 1j * res["fp64"]["topk"]["y"]))
+    vtc = dict(zip(ktc.tolist(), res["tc"]["topk"]["x"] + 1j * res["tc"]["topk"]["y"]))
+    a = np.array([v64[kk] for kk in k64.tolist()])
+    b = np.array([vtc[kk] for kk in k64.tolist()])
+    assert np.linalg.norm(a - b) / np.linalg.norm(a) <= 1e-5
