@@ -492,8 +492,9 @@ int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch) {
   return GSFFT_OK;
 }
 
-// FP32 plan whose last two passes are radix-64 tensor-core passes: n = 2^L
-// with a CUDA-core first pass of radix 2^(L-12) (5 <= L-12 <= 14).
+// FP32 plan whose first pass is a radix-4096 tensor-core pass (two DFT_64
+// stages; its outputs are then contiguous) and whose second is a CUDA-core
+// pass of radix 2^(L-12): n = 2^L, 5 <= L-12 <= 14.
 int fft_plan_init_tc(FftPlan &p, long long n, int max_batch) {
   fft_plan_free(p);
   if (n < 256 || (n & (n - 1)) != 0) return GSFFT_ERR_UNSUPPORTED;
@@ -503,12 +504,11 @@ int fft_plan_init_tc(FftPlan &p, long long n, int max_batch) {
   p.n = n;
   p.L = L;
   p.precision = GSFFT_MIXED;
-  p.npass = 3;
-  p.logR[0] = L - 12;
-  p.logR[1] = 6;
-  p.logR[2] = 6;
-  p.tc[0] = false;
-  p.tc[1] = p.tc[2] = true;
+  p.npass = 2;
+  p.logR[0] = 12;
+  p.logR[1] = L - 12;
+  p.tc[0] = true;
+  p.tc[1] = false;
   long long Np = 1;
   for (int i = 0; i < p.npass; i++) {
     const long long R = 1LL << p.logR[i];
@@ -523,7 +523,7 @@ int fft_plan_init_tc(FftPlan &p, long long n, int max_batch) {
     GS_CHECK(make_table<float>(&p.tw_R[i], R, 1, R));
   }
   GS_CHECK(tc_build_F(&p.tc_F));
-  p.scratch_elems = (long long)n * max_batch * 2;
+  p.scratch_elems = (long long)n * max_batch;
   GS_CUDA(cudaMalloc(&p.scratch, sizeof(float2) * p.scratch_elems));
   GS_CUDA(cudaDeviceSynchronize());
   return GSFFT_OK;
@@ -592,7 +592,7 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
     a.total = total_sub;
     int s;
     if (p.tc[i]) {
-      if (i == 0 || dbl) return GSFFT_ERR_UNSUPPORTED;  // no gather / partial loader here
+      if (dbl || a.gx || p.logR[i] != 12) return GSFFT_ERR_UNSUPPORTED;  // partial sums, no gather
       TcPassArgs t;
       t.in = a.in;
       t.out = a.out;
@@ -605,11 +605,14 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
       t.tw_lo = a.tw_lo;
       t.tw_h = a.tw_h;
       t.F = p.tc_F;
+      t.tw_R = p.tw_R[i];
       t.samples = a.samples;
       t.row_max = a.row_max;
       t.write_complex = a.write_complex;
       t.err = io.err;
-      s = launch_tc_pass(t, st);
+      t.nsum = a.nsum;
+      t.sstride = a.sstride;
+      s = launch_tc4096_pass(t, st);
     } else {
       s = dbl ? dispatch_pass<double>(p.logR[i], a, total_sub, st)
               : dispatch_pass<float>(p.logR[i], a, total_sub, st);

@@ -78,13 +78,13 @@ struct FftPlan {
   void *tw_lo[3] = {nullptr, nullptr, nullptr};
   int tw_h[3] = {0, 0, 0};
   void *tw_R[3] = {nullptr, nullptr, nullptr};  // exp(-2 pi i m / R) for the pass radix
-  bool tc[3] = {false, false, false};  // pass runs on the tensor cores (radix 64, FP32)
+  bool tc[3] = {false, false, false};  // pass runs on the tensor cores (radix 4096, FP32)
   void *tc_F = nullptr;                // DFT_64 operand of the tensor-core passes
   void *scratch = nullptr; // one transform-sized buffer per batch entry (multi-pass)
   long long scratch_elems = 0;
 };
 
-// One radix-64 pass of an FP32 FFT on the tensor cores (tc_dft.cu).
+// One radix-4096 pass of an FP32 FFT on the tensor cores (tc_dft.cu).
 struct TcPassArgs {
   const void *in;       // float2
   void *out;            // float2
@@ -94,13 +94,17 @@ struct TcPassArgs {
   const void *tw_hi, *tw_lo;
   int tw_h;
   const void *F;        // three bf16 parts of the DFT_64 real form (tc_build_F)
+  const void *tw_R;     // exp(-2 pi i m / 4096) for the radix-4096 form
   void *samples;        // float |X|^2 or null
   void *row_max;        // u32 bit pattern per row, with samples
   int write_complex;
   int *err;             // set when a completion wait timed out (may be null)
+  int nsum = 1;         // radix-4096 form: add nsum partial inputs sstride apart
+  long long sstride = 0;
 };
 int tc_build_F(void **F);
-int launch_tc_pass(const TcPassArgs &a, cudaStream_t st);
+// radix 4096 = 64 x 64 in one pass (four-step, both DFT_64 stages on the tensor cores)
+int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st);
 
 // Optional fused prologue/epilogue of an FFT execution.
 struct FftIo {
@@ -123,8 +127,8 @@ struct FftIo {
 };
 
 int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch);
-// FP32 plan with radix-64 tensor-core passes (last two); GSFFT_ERR_UNSUPPORTED
-// when n does not decompose as 2^(5..14) x 64 x 64
+// FP32 plan: radix-4096 tensor-core pass, then a CUDA-core pass of radix
+// n / 4096; GSFFT_ERR_UNSUPPORTED unless n = 2^(17..26)
 int fft_plan_init_tc(FftPlan &p, long long n, int max_batch);
 void fft_plan_free(FftPlan &p);
 // in: batch entries at in + b*n; out: out + b*n.  sign -1 forward, +1 inverse.

@@ -222,32 +222,109 @@ constexpr int TP_THREADS = 256;  // two warpgroups: TMEM quadrant = warp % 4
 constexpr int DP = 68;           // row pitch (floats) of the fp32 result staged in shared memory
 static_assert(128 * DP * 4 <= 3 * B_BYTES, "result staging fits the X parts");
 
-__device__ __forceinline__ unsigned pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-  return (unsigned)__bfloat16_as_ushort(lo) | ((unsigned)__bfloat16_as_ushort(hi) << 16);
+
+constexpr int ST_BYTES = 128 * DP * 4;  // fp32 staging of a 128 x 64 result
+constexpr int TC4K_SMEM = 3 * A_BYTES + 3 * B_BYTES + ST_BYTES + 64;
+
+// issue the six bf16 products D = F * X (X parts at xb) and commit to bar;
+// returns false when F did not arrive in time (nothing issued then)
+__device__ __forceinline__ void tc_issue(unsigned char *A, unsigned char *xb, unsigned tmem, unsigned bar) {
+  constexpr unsigned IDESC = idesc_bf16(TC_M, TC_N);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const int pa[6] = {1, 0, 2, 0, 1, 0};
+  const int pb[6] = {1, 2, 0, 1, 0, 0};
+  for (int t = 0; t < 6; t++) {
+    const unsigned abase = smem_addr(A + pa[t] * A_BYTES);
+    const unsigned bbase = smem_addr(xb + pb[t] * B_BYTES);
+#pragma unroll
+    for (int kk = 0; kk < TC_K / 16; kk++) {
+      const unsigned long long ad = smem_desc(abase + kk * 256, 128, (TC_K / 8) * 128);
+      const unsigned long long bd = smem_desc(bbase + kk * 256, 128, (TC_K / 8) * 128);
+      const unsigned acc = (t > 0 || kk > 0) ? 1u : 0u;
+      asm volatile(
+          "{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem),
+          "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+          : "memory");
+    }
+  }
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
 }
 
-// One radix-64 Stockham pass of an FP32 FFT (the index scheme of
-// fft_pass_kernel): sub-transform u of batch row b = u / S takes
-// v[r] = in[j + r S] * w((j mod Ns) r / (Ns 64)), V = DFT_64(v),
-// out[(j / Ns) Ns 64 + (j mod Ns) + k Ns] = V[k].  64 sub-transforms per
-// tile; persistent CTAs.  F arrives by one bulk copy overlapping the first
-// tile's loads.
-__global__ void __launch_bounds__(TP_THREADS, 1) tc_pass_kernel(TcPassArgs a) {
+// TMEM result (128 lanes x 64 columns) -> stg[m][c] (row pitch DP), by 8 warps
+__device__ __forceinline__ void tmem_to_stage(unsigned tmem, float *stg, int warp, int lane) {
+  const int q4 = warp & 3, h = warp >> 2;
+  const int m = 32 * q4 + lane;
+#pragma unroll
+  for (int c = 0; c < 32; c += 8) {
+    const int c0 = 32 * h + c;
+    unsigned r[8];
+    const unsigned taddr = tmem + ((unsigned)(32 * q4) << 16) + (unsigned)c0;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    uint4 *d4 = reinterpret_cast<uint4 *>(stg + m * DP + c0);
+    d4[0] = make_uint4(r[0], r[1], r[2], r[3]);
+    d4[1] = make_uint4(r[4], r[5], r[6], r[7]);
+  }
+}
+
+// split eight complex values into the three bf16 parts of operand row `row`,
+// columns kc..kc+7 (re) and 64+kc..64+kc+7 (im)
+__device__ __forceinline__ void store_parts8(unsigned char *xb, int row, int kc, const float2 (&x)[8]) {
+  unsigned wr[3][4], wi[3][4];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    __nv_bfloat16 r[3], im[3];
+    split3(x[q].x, r[0], r[1], r[2]);
+    split3(x[q].y, im[0], im[1], im[2]);
+#pragma unroll
+    for (int pp = 0; pp < 3; pp++) {
+      const unsigned br = __bfloat16_as_ushort(r[pp]), bi = __bfloat16_as_ushort(im[pp]);
+      if (q & 1) {
+        wr[pp][q >> 1] |= br << 16;
+        wi[pp][q >> 1] |= bi << 16;
+      } else {
+        wr[pp][q >> 1] = br;
+        wi[pp][q >> 1] = bi;
+      }
+    }
+  }
+  const int offr = kmajor_off(row, kc, TC_K), offi = kmajor_off(row, 64 + kc, TC_K);
+#pragma unroll
+  for (int pp = 0; pp < 3; pp++) {
+    *reinterpret_cast<uint4 *>(xb + pp * B_BYTES + offr) = make_uint4(wr[pp][0], wr[pp][1], wr[pp][2], wr[pp][3]);
+    *reinterpret_cast<uint4 *>(xb + pp * B_BYTES + offi) = make_uint4(wi[pp][0], wi[pp][1], wi[pp][2], wi[pp][3]);
+  }
+}
+
+// One radix-4096 Stockham pass of an FP32 FFT as a four-step transform on the
+// tensor cores: one sub-transform per tile; with r = r1 + 64 r2 and
+// k = k2 + 64 k1,
+//   Y[r1][k2] = sum_r2 v[r1 + 64 r2] W64^(r2 k2)            (tensor cores)
+//   V[k2 + 64 k1] = sum_r1 W64^(r1 k1) W4096^(r1 k2) Y[r1][k2] (tensor cores)
+// where v[r] = in[j + r S] * w((j mod Ns) r / (Ns 4096)) and the result goes
+// to out[(j / Ns) Ns 4096 + (j mod Ns) + k Ns].
+__global__ void __launch_bounds__(TP_THREADS, 1) tc4096_pass_kernel(TcPassArgs a) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   unsigned char *A = tsm;
-  unsigned char *Bm = tsm + 3 * A_BYTES;               // X parts; reused as the fp32 result
-  float *D = reinterpret_cast<float *>(Bm);            // [128][DP]
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tsm + 3 * A_BYTES + 3 * B_BYTES);
-  unsigned long long *fbar = bar + 1;                  // F arrival
+  unsigned char *Bm = tsm + 3 * A_BYTES;
+  float *stg = reinterpret_cast<float *>(tsm + 3 * A_BYTES + 3 * B_BYTES);  // [128][DP]
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tsm + 3 * A_BYTES + 3 * B_BYTES + ST_BYTES);
+  unsigned long long *fbar = bar + 1;
   unsigned *tmem_slot = reinterpret_cast<unsigned *>(bar + 2);
-  unsigned *red = tmem_slot + 1;                       // [8] warp maxima
+  unsigned *red = tmem_slot + 1;  // [8]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const float2 *__restrict__ in = reinterpret_cast<const float2 *>(a.in);
   float2 *__restrict__ out = reinterpret_cast<float2 *>(a.out);
   float *__restrict__ smp = reinterpret_cast<float *>(a.samples);
   const float2 *__restrict__ thi = reinterpret_cast<const float2 *>(a.tw_hi);
   const float2 *__restrict__ tlo = reinterpret_cast<const float2 *>(a.tw_lo);
-  const int logS = a.logN - 6;
+  const float2 *__restrict__ t4k = reinterpret_cast<const float2 *>(a.tw_R);  // exp(-2 pi i m / 4096)
+  const int logS = a.logN - 12;
   const long long Smask = (1LL << logS) - 1;
   const int logNs = a.logNs;
   const long long Nsmask = (1LL << logNs) - 1;
@@ -263,7 +340,6 @@ __global__ void __launch_bounds__(TP_THREADS, 1) tc_pass_kernel(TcPassArgs a) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(fbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    // F: one 96 KiB bulk copy, completion counted on fbar
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(fbar)),
                  "r"(3 * A_BYTES)
                  : "memory");
@@ -277,145 +353,103 @@ __global__ void __launch_bounds__(TP_THREADS, 1) tc_pass_kernel(TcPassArgs a) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const unsigned tmem = *tmem_slot;
-  constexpr unsigned IDESC = idesc_bf16(TC_M, TC_N);
   unsigned phase = 0;
   bool ok = true, f_ready = false;
-  const long long tiles = (a.total + TC_N - 1) / TC_N;
 
-  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-    const long long u0 = tile * TC_N;
-    // ---- load: two items (v, eight consecutive r) per thread, all 16 loads in flight
-    float2 xv[2][8];
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
-      const int item = tid + it * TP_THREADS;
-      const int v = item & 63, r0 = (item >> 6) * 8;
-      const long long u = u0 + v;
-      const bool live = u < a.total;
-      const long long b = live ? (u >> logS) : 0, j = live ? (u & Smask) : 0;
-#pragma unroll
-      for (int q = 0; q < 8; q++)
-        xv[it][q] = live ? in[b * a.bstride + j + ((long long)(r0 + q) << logS)] : make_float2(0.f, 0.f);
-    }
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
-      const int item = tid + it * TP_THREADS;
-      const int v = item & 63, r0 = (item >> 6) * 8;
-      const long long u = u0 + v;
-      const long long j = u & Smask;
-      unsigned wr[3][4], wi[3][4];
-#pragma unroll
-      for (int q = 0; q < 8; q++) {
-        float2 x = xv[it][q];
-        if (a.inverse) x.y = -x.y;
-        if (logNs > 0) {
-          const long long mm = (j & Nsmask) * (r0 + q);
-          x = cmul(x, cmul(thi[mm >> a.tw_h], tlo[mm & hmask]));
-        }
-        __nv_bfloat16 r[3], im[3];
-        split3(x.x, r[0], r[1], r[2]);
-        split3(x.y, im[0], im[1], im[2]);
-        if (q & 1) {
-#pragma unroll
-          for (int pp = 0; pp < 3; pp++) {
-            wr[pp][q >> 1] |= (unsigned)__bfloat16_as_ushort(r[pp]) << 16;
-            wi[pp][q >> 1] |= (unsigned)__bfloat16_as_ushort(im[pp]) << 16;
-          }
-        } else {
-#pragma unroll
-          for (int pp = 0; pp < 3; pp++) {
-            wr[pp][q >> 1] = __bfloat16_as_ushort(r[pp]);
-            wi[pp][q >> 1] = __bfloat16_as_ushort(im[pp]);
-          }
-        }
-      }
-      const int offr = kmajor_off(v, r0, TC_K), offi = kmajor_off(v, 64 + r0, TC_K);
-#pragma unroll
-      for (int pp = 0; pp < 3; pp++) {
-        *reinterpret_cast<uint4 *>(Bm + pp * B_BYTES + offr) = make_uint4(wr[pp][0], wr[pp][1], wr[pp][2], wr[pp][3]);
-        *reinterpret_cast<uint4 *>(Bm + pp * B_BYTES + offi) = make_uint4(wi[pp][0], wi[pp][1], wi[pp][2], wi[pp][3]);
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    // ---- six bf16 products into TMEM
-    if (tid == 0) {
-      bool go = true;
-      if (!f_ready) {
-        go = mbar_wait_bounded(smem_addr(fbar), 0);
-        f_ready = go;
-      }
-      if (go) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int pa[6] = {1, 0, 2, 0, 1, 0};
-        const int pb[6] = {1, 2, 0, 1, 0, 0};
-        for (int t = 0; t < 6; t++) {
-          const unsigned abase = smem_addr(A + pa[t] * A_BYTES);
-          const unsigned bbase = smem_addr(Bm + pb[t] * B_BYTES);
-#pragma unroll
-          for (int kk = 0; kk < TC_K / 16; kk++) {
-            const unsigned long long ad = smem_desc(abase + kk * 256, 128, (TC_K / 8) * 128);
-            const unsigned long long bd = smem_desc(bbase + kk * 256, 128, (TC_K / 8) * 128);
-            const unsigned acc = (t > 0 || kk > 0) ? 1u : 0u;
-            asm volatile(
-                "{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem),
-                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
-                : "memory");
-          }
-        }
-      }
-      // the commit arrives even when nothing was issued, so the wait below ends
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_addr(bar))
-                   : "memory");
-      if (!go) {
-        ok = false;
-        if (a.err) atomicExch(a.err, 1);
-      }
-    }
-    if (!mbar_wait_bounded(smem_addr(bar), phase)) {
-      ok = false;
-      if (tid == 0 && a.err) atomicExch(a.err, 1);
-    }
-    ok = __syncthreads_and(ok) != 0;
-    phase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (!ok) break;
-    // ---- TMEM -> shared memory: warp w reads quadrant w % 4, columns 32 (w / 4) ..
+  for (long long u = blockIdx.x; u < a.total && ok; u += gridDim.x) {
+    const long long b = u >> logS, j = u & Smask;
+    const float2 *src = in + b * a.bstride + j;
+    // ---- step 1 operand: row r1, columns r2 (eight per item)
     {
-      const int q4 = warp & 3, h = warp >> 2;
-      const int m = 32 * q4 + lane;
+      float2 xv[2][8];
 #pragma unroll
-      for (int c = 0; c < 32; c += 8) {
-        const int c0 = 32 * h + c;
-        unsigned r[8];
-        const unsigned taddr = tmem + ((unsigned)(32 * q4) << 16) + (unsigned)c0;
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        uint4 *d4 = reinterpret_cast<uint4 *>(D + m * DP + c0);
-        d4[0] = make_uint4(r[0], r[1], r[2], r[3]);
-        d4[1] = make_uint4(r[4], r[5], r[6], r[7]);
+      for (int it = 0; it < 2; it++) {
+        const int item = tid + it * TP_THREADS;
+        const int r1 = item & 63, g = item >> 6;
+#pragma unroll
+        for (int q = 0; q < 8; q++) xv[it][q] = src[(long long)(r1 + 64 * (8 * g + q)) << logS];
+        // row-group partial inputs (first pass after the streaming perm+filter),
+        // added in group order
+        for (int s2 = 1; s2 < a.nsum; s2++)
+#pragma unroll
+          for (int q = 0; q < 8; q++)
+            xv[it][q] = cadd(xv[it][q], src[s2 * a.sstride + ((long long)(r1 + 64 * (8 * g + q)) << logS)]);
+      }
+#pragma unroll
+      for (int it = 0; it < 2; it++) {
+        const int item = tid + it * TP_THREADS;
+        const int r1 = item & 63, g = item >> 6;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          float2 x = xv[it][q];
+          if (a.inverse) x.y = -x.y;
+          if (logNs > 0) {
+            const long long mm = (j & Nsmask) * (long long)(r1 + 64 * (8 * g + q));
+            x = cmul(x, cmul(thi[mm >> a.tw_h], tlo[mm & hmask]));
+          }
+          xv[it][q] = x;
+        }
+        store_parts8(Bm, r1, 8 * g, xv[it]);
       }
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    // ---- outputs: (v fast, k) pairs, complex and/or |X|^2
+    for (int step = 0; step < 2 && ok; step++) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        bool go = true;
+        if (!f_ready) {
+          go = mbar_wait_bounded(smem_addr(fbar), 0);
+          f_ready = go;
+        }
+        if (go) {
+          tc_issue(A, Bm, tmem, smem_addr(bar));
+        } else {
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_addr(bar))
+                       : "memory");
+          ok = false;
+          if (a.err) atomicExch(a.err, 1);
+        }
+      }
+      if (!mbar_wait_bounded(smem_addr(bar), phase)) {
+        ok = false;
+        if (tid == 0 && a.err) atomicExch(a.err, 1);
+      }
+      ok = __syncthreads_and(ok) != 0;
+      phase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (!ok) break;
+      tmem_to_stage(tmem, stg, warp, lane);  // stg[m][c]: m = output (re | im), c = vector
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      if (step == 0) {
+        // step 3 operand: row k2, columns r1: Z = Y[r1][k2] * W4096^(r1 k2)
+#pragma unroll
+        for (int it = 0; it < 2; it++) {
+          const int item = tid + it * TP_THREADS;
+          const int k2 = item & 63, g = item >> 6;
+          float2 z[8];
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const int r1 = 8 * g + q;
+            const float2 y = make_float2(stg[k2 * DP + r1], stg[(64 + k2) * DP + r1]);
+            z[q] = cmul(y, __ldg(&t4k[(r1 * k2) & 4095]));
+          }
+          store_parts8(Bm, k2, 8 * g, z);
+        }
+      }
+    }
+    if (!ok) break;
+    // ---- outputs: k = k2 + 64 k1; stg[k1 (re) | 64 + k1 (im)][k2]
     float tmax = 0.f;
-    const long long b_tile = u0 >> logS;  // S >= 64: the tile lies in one batch row
 #pragma unroll 4
-    for (int e = tid; e < TC_N * 64; e += TP_THREADS) {
-      const int v = e & 63, k = e >> 6;
-      const long long u = u0 + v;
-      if (u >= a.total) continue;
-      const long long j = u & Smask;
-      const float re = D[k * DP + v];
-      float im = D[(64 + k) * DP + v];
+    for (int e = tid; e < 4096; e += TP_THREADS) {
+      const int k2 = e & 63, k1 = e >> 6;
+      const int k = k2 + 64 * k1;
+      const float re = stg[k1 * DP + k2];
+      float im = stg[(64 + k1) * DP + k2];
       if (a.inverse) im = -im;
-      const long long dest = (u >> logS) * a.bstride + ((j >> logNs) << (logNs + 6)) + (j & Nsmask) +
+      const long long dest = b * a.bstride + ((j >> logNs) << (logNs + 12)) + (j & Nsmask) +
                              ((long long)k << logNs);
       if (a.write_complex) out[dest] = make_float2(re, im);
       if (smp) {
@@ -436,12 +470,11 @@ __global__ void __launch_bounds__(TP_THREADS, 1) tc_pass_kernel(TcPassArgs a) {
       if (tid == 0) {
         unsigned m8 = red[0];
         for (int w2 = 1; w2 < TP_THREADS / 32; w2++) m8 = red[w2] > m8 ? red[w2] : m8;
-        atomicMax(reinterpret_cast<unsigned *>(a.row_max) + b_tile, m8);
+        atomicMax(reinterpret_cast<unsigned *>(a.row_max) + b, m8);
       }
     }
-    __syncthreads();  // the result staging and X parts are rewritten by the next tile
+    __syncthreads();  // the staging and operand buffers are rewritten by the next tile
   }
-  // a CTA without tiles (or stopped early) still owns the F copy: wait for it
   if (tid == 0 && !f_ready) (void)mbar_wait_bounded(smem_addr(fbar), 0);
   __syncthreads();
   if (warp == 0)
@@ -474,22 +507,22 @@ int tc_build_F(void **F) {
   return GSFFT_OK;
 }
 
-int launch_tc_pass(const TcPassArgs &a, cudaStream_t st) {
+int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    GS_CUDA(cudaFuncSetAttribute(tc_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    GS_CUDA(cudaFuncSetAttribute(tc4096_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC4K_SMEM));
     attr = true;
   }
-  if (a.logN - 6 < 6) return GSFFT_ERR_UNSUPPORTED;  // a tile of 64 must stay inside one row
+  if (a.logN < 12 || !a.tw_R) return GSFFT_ERR_UNSUPPORTED;
   int dev = 0, sms = 0;
   GS_CUDA(cudaGetDevice(&dev));
   GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const long long tiles = (a.total + TC_N - 1) / TC_N;
-  const int grid = (int)(tiles < sms ? tiles : sms);
+  const int grid = (int)(a.total < sms ? a.total : sms);
   if (grid < 1) return GSFFT_OK;
-  tc_pass_kernel<<<grid, TP_THREADS, TC_SMEM, st>>>(a);
+  tc4096_pass_kernel<<<grid, TP_THREADS, TC4K_SMEM, st>>>(a);
   GS_LAUNCHED();
   return GSFFT_OK;
 }
+
 
 }  // namespace gsfft

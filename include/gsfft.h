@@ -62,9 +62,10 @@ typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
    would move fewer DRAM bytes */
 #define GSFFT_FLAG_FORCE_STREAM 8u   /* perm+filter (and the RLFC sub-sampling) by
    one ordered pass over the signal whenever the sizes allow it */
-#define GSFFT_FLAG_TC_BUCKET_FFT 16u /* MIXED: the B-point bucket FFT with its
-   last two radix-64 passes on the tensor cores (tcgen05, three-part bf16
-   split products accumulated in fp32) when B = 2^(5..14) x 64 x 64 */
+#define GSFFT_FLAG_TC_BUCKET_FFT 16u /* MIXED: the B-point bucket FFT as a
+   radix-2^(L-12) pass and a 4096-point four-step pass whose two DFT_64 stages
+   run on the tensor cores (tcgen05, three-part bf16 split products
+   accumulated in fp32), when B = 2^L with 17 <= L <= 26 */
 
 /* Run parameters derived exactly as experiment.c:71-84 and
  * cuExperiment.cu:279-284 derive them. */

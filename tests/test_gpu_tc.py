@@ -22,7 +22,7 @@ def test_tc_dft64_matches_numpy(G, torch_cuda, nvec):
 
 
 def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
-    """Mixed engine with the tensor-core bucket FFT (B = 2^17 = 32 x 64 x 64)
+    """Mixed engine with the tensor-core bucket FFT (B = 2^17 = 32 x 4096)
     against the CUDA-core mixed engine and the FP64 engine, same draws."""
     from gsfft import synth
     torch = torch_cuda
@@ -48,7 +48,7 @@ def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
         r["launches"] = plan.launches_per_run()
         plan.close()
         res[name] = r
-    assert res["tc"]["launches"] == res["mixed"]["launches"] + 1  # three bucket-FFT passes
+    assert res["tc"]["launches"] == res["mixed"]["launches"]  # two bucket-FFT passes either way
     b_tc = res["tc"]["bins"].astype(np.complex128)
     b_cc = res["mixed"]["bins"].astype(np.complex128)
     assert np.linalg.norm(b_tc - b_cc) / np.linalg.norm(b_cc) < 1e-5
