@@ -20,7 +20,7 @@
 // ascending row (= signal position) order: fixed, no atomics.
 //
 // Tiles of rt rows x 128 columns arrive by cp.async.bulk.tensor.2d, issued
-// by a producer warp, into a six-stage shared-memory ring guarded by full /
+// by a producer warp, into a three-stage shared-memory ring guarded by full /
 // empty mbarriers whose waits are bounded (a timeout sets an error flag
 // instead of hanging).
 //
@@ -40,7 +40,7 @@ namespace gsfft {
 namespace {
 
 constexpr int ST = 128;      // B must be a multiple of this
-constexpr int NSTAGE = 6;    // shared-memory ring of tiles
+constexpr int NSTAGE = 3;    // shared-memory ring of tiles
 constexpr int MAXT = 32;     // full tiles of taps per bucket (w / B) supported
 constexpr int MAXL = 16;     // loops supported
 constexpr int PFD = 1;        // filter taps loaded ahead per thread
@@ -484,7 +484,7 @@ bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops) {
 }
 
 static int stream_rows_per_tile(int n, int B, int precision) {
-  return std::min(n / B, precision == GSFFT_FP64 ? 16 : 32);  // 16 KiB tiles of 64 columns
+  return std::min(n / B, precision == GSFFT_FP64 ? 32 : 64);  // 32 KiB tiles of 64 columns
 }
 
 int stream_pf_groups(int n, int B, int loops, int precision) {

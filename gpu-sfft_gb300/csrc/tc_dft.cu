@@ -220,14 +220,11 @@ __global__ void tc_build_F_kernel(unsigned char *F) {
 
 constexpr int TP_THREADS = 256;  // two warpgroups: TMEM quadrant = warp % 4
 constexpr int DP = 68;           // row pitch (floats) of the fp32 result staged in shared memory
-static_assert(128 * DP * 4 <= 3 * B_BYTES, "result staging fits the X parts");
-
 
 constexpr int ST_BYTES = 128 * DP * 4;  // fp32 staging of a 128 x 64 result
 constexpr int TC4K_SMEM = 3 * A_BYTES + 3 * B_BYTES + ST_BYTES + 64;
 
-// issue the six bf16 products D = F * X (X parts at xb) and commit to bar;
-// returns false when F did not arrive in time (nothing issued then)
+// issue the six bf16 products D = F * X (X parts at xb) and commit them to bar
 __device__ __forceinline__ void tc_issue(unsigned char *A, unsigned char *xb, unsigned tmem, unsigned bar) {
   constexpr unsigned IDESC = idesc_bf16(TC_M, TC_N);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
