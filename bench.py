@@ -223,7 +223,7 @@ def useful_bytes(p, es):
 # captures summarised under profiles/ (keyed by kernel, form and workload):
 # profiles/pf_tma_kernel_stream_perm_filter.md.
 TRAFFIC = {
-    ("perm_filter", "stream", "q27k16000"): int(1.10e9 + 28.59e6),
+    ("perm_filter", "stream", "q27k16000"): 1100303360 + 29271552,
 }
 
 
