@@ -93,11 +93,21 @@ template <typename T> __host__ __device__ constexpr int minb_of(int logr) {
              : (sizeof(T) == 4 ? (nt_of<T>(logr) >= 512 ? 2 : 4) : (nt_of<T>(logr) >= 512 ? 1 : 2));
 }
 __host__ __device__ constexpr int padded(int i) { return i + (i >> 4); }
-// row stride in elements: one extra element so the G rows start in different banks
-__host__ __device__ constexpr int rowpitch(int logr) { return padded(1 << logr) + 1; }
+// Row stride in elements.  Rows start in different banks; when a warp's load
+// or store phase interleaves G rows (FP32, 2 <= G <= 16, each row handled by
+// whole warps in the butterfly stages), a pitch of 32/G 8-byte elements past
+// a multiple of 16 makes the G x (32/G) lanes fill every bank pair exactly
+// twice (two wavefronts) instead of colliding.
+template <typename T> __host__ __device__ constexpr int rowpitch(int logr) {
+  return padded(1 << logr) +
+         ((sizeof(T) == 4 && g_of<T>(logr) >= 2 && g_of<T>(logr) <= 16 &&
+           nt_of<T>(logr) / g_of<T>(logr) >= 32)
+              ? 32 / g_of<T>(logr)
+              : 1);
+}
 // twiddle table exp(-2 pi i m / R) copied into shared memory when it fits
 template <typename T> __host__ __device__ constexpr int data_smem_of(int logr) {
-  return g_of<T>(logr) * rowpitch(logr) * (int)sizeof(typename Cx<T>::V);
+  return g_of<T>(logr) * rowpitch<T>(logr) * (int)sizeof(typename Cx<T>::V);
 }
 template <typename T> __host__ __device__ constexpr bool tw_in_smem(int logr) {
   return data_smem_of<T>(logr) + (1 << logr) * (int)sizeof(typename Cx<T>::V) <= 220 * 1024;
@@ -111,7 +121,7 @@ template <typename T> __host__ __device__ constexpr int smem_of(int logr) {
 template <typename V, int LOGR, int G, int E>
 __device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR, int Ns) {
   constexpr int R = 1 << LOGR;
-  constexpr int RP = rowpitch(LOGR);
+  constexpr int RP = rowpitch<decltype(V().x)>(LOGR);
   constexpr int NT = imin((R / 16) * G, 512);
   constexpr int TPF = NT / G;
   constexpr int NB = R / E;          // butterflies per row
@@ -232,7 +242,7 @@ __device__ __forceinline__ void row_max_update(void *rm, long long b, float v) {
 template <typename T, int LOGR>
 __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   typedef typename Cx<T>::V V;
-  constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = rowpitch(LOGR);
+  constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = rowpitch<T>(LOGR);
   constexpr int ITER = R * G / NT;  // elements per thread in the load / store phases
   extern __shared__ __align__(16) unsigned char smraw[];
   V *sm = reinterpret_cast<V *>(smraw);
