@@ -20,27 +20,44 @@ namespace {
 
 constexpr int ET = 128;
 
+// Order-preserving integer key of a double (finite values): comparing keys
+// as unsigned integers orders the values, so the ranking below runs on the
+// integer pipe instead of GB300's narrow FP64 pipe.  (-0.0 ranks just below
+// +0.0; both are the same value.)
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Element (L-1)/2 of the ascending order (ties by index), by rank counting.
 __device__ __forceinline__ double median_of(const double *v, int L) {
   const int want = (L - 1) / 2;
   double res = v[0];
   for (int i = 0; i < L; i++) {
+    const unsigned long long ki = dkey(v[i]);
     int rank = 0;
-    for (int j = 0; j < L; j++) rank += (v[j] < v[i]) || (v[j] == v[i] && j < i);
+    for (int j = 0; j < L; j++) {
+      const unsigned long long kj = dkey(v[j]);
+      rank += (kj < ki) || (kj == ki && j < i);
+    }
     if (rank == want) res = v[i];
   }
   return res;
 }
 
-// Compile-time loop count: the per-loop values live in registers.
+// Compile-time loop count: the per-loop values and keys live in registers.
 template <int L>
 __device__ __forceinline__ double median_reg(const double (&v)[L]) {
   constexpr int want = (L - 1) / 2;
+  unsigned long long k[L];
+#pragma unroll
+  for (int i = 0; i < L; i++) k[i] = dkey(v[i]);
   double res = v[0];
 #pragma unroll
   for (int i = 0; i < L; i++) {
     int rank = 0;
 #pragma unroll
-    for (int j = 0; j < L; j++) rank += (v[j] < v[i]) || (v[j] == v[i] && j < i);
+    for (int j = 0; j < L; j++) rank += (k[j] < k[i]) || (k[j] == k[i] && j < i);
     if (rank == want) res = v[i];
   }
   return res;
