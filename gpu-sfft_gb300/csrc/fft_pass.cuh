@@ -218,6 +218,78 @@ __device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR) {
   __syncthreads();
 }
 
+// Radices up to 2^9 (G >= 8 rows per CTA): the same stages with Ns at run time
+// in one loop -- fully inlined compile-time stages spill there under the
+// 64-register budget of four resident CTAs.
+template <typename V, int LOGR, int G, int E>
+__device__ __forceinline__ void rt_smem_stage(V *sm, const V *__restrict__ twR, int Ns) {
+  constexpr int R = 1 << LOGR;
+  constexpr int RP = rowpitch<decltype(V().x)>(LOGR);
+  constexpr int NT = imin((R / 16) * G, 512);
+  constexpr int TPF = NT / G;
+  constexpr int NB = R / E;          // butterflies per row
+  constexpr int Q = NB / TPF;        // butterflies per thread
+  const int g = threadIdx.x / TPF, t0 = threadIdx.x % TPF;
+  V *s = sm + g * RP;
+  V v[Q][E];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int t = t0 + q * TPF;
+#pragma unroll
+    for (int e = 0; e < E; e++) v[q][e] = s[padded(t + e * NB)];
+    if (Ns > 1) {
+      const int k = t % Ns;
+      const int step = R / (Ns * E);
+      if (sizeof(v[0][0].x) == 8 || E < 4) {
+        // FP64: exact table entries (its FP64 pipe, not shared memory, is the limit)
+#pragma unroll
+        for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], twR[k * e * step]);
+      } else {
+        // FP32: two table reads (w, w^4), other powers by products at most four
+        // deep -- the strided table reads were the shared-memory bank hot spot
+        V w[E];
+        w[1] = twR[k * step];
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
+        w[4] = twR[4 * k * step];
+#pragma unroll
+        for (int e = 5; e < 8 && e < E; e++) w[e] = cmul(w[4], w[e - 4]);
+        if (E == 16) {
+          w[8] = cmul(w[4], w[4]);
+#pragma unroll
+          for (int e = 9; e < 12; e++) w[e] = cmul(w[8], w[e - 8]);
+          w[12] = cmul(w[8], w[4]);
+#pragma unroll
+          for (int e = 13; e < 16; e++) w[e] = cmul(w[12], w[e - 12]);
+        }
+#pragma unroll
+        for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], w[e]);
+      }
+    }
+    dft_reg<V, E>(v[q]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int t = t0 + q * TPF;
+    const int base = (t / Ns) * Ns * E + (t % Ns);
+#pragma unroll
+    for (int e = 0; e < E; e++) s[padded(base + e * Ns)] = v[q][bitrev<E>(e)];
+  }
+  __syncthreads();
+}
+
+template <typename V, int LOGR, int G>
+__device__ __forceinline__ void rt_cta_fft(V *sm, const V *__restrict__ twR) {
+  constexpr int LEFT = LOGR % 4;
+  int Ns = 1;
+  if (LEFT == 1) { rt_smem_stage<V, LOGR, G, 2>(sm, twR, Ns); Ns <<= 1; }
+  if (LEFT == 2) { rt_smem_stage<V, LOGR, G, 4>(sm, twR, Ns); Ns <<= 2; }
+  if (LEFT == 3) { rt_smem_stage<V, LOGR, G, 8>(sm, twR, Ns); Ns <<= 3; }
+#pragma unroll 1
+  for (int s = 0; s < LOGR / 4; s++) { rt_smem_stage<V, LOGR, G, 16>(sm, twR, Ns); Ns <<= 4; }
+}
+
 template <typename V, int LOGR, int G, int LOGNS>
 __device__ __forceinline__ void radix16_stages(V *sm, const V *__restrict__ twR) {
   if constexpr (LOGNS + 4 <= LOGR) {
@@ -234,6 +306,36 @@ __device__ __forceinline__ void cta_fft(V *sm, const V *__restrict__ twR) {
   if constexpr (LEFT == 3) smem_stage<V, LOGR, G, 8, 0>(sm, twR);
   radix16_stages<V, LOGR, G, LEFT>(sm, twR);
 }
+
+// FP32 inter-pass twiddles W^(jm r), r = r0 + q TPF, q = 0, 1, ... in order,
+// of one thread: three two-level table look-ups -- W^(jm r0), W^(jm TPF),
+// W^(4 jm TPF) -- instead of one per element, then
+//   w_q = A_(q/4) B_(q mod 4),  A_0 = W^(jm r0), A_m = A_(m-1) W^(4 jm TPF),
+//   B_i = W^(i jm TPF),
+// so w_q is within about q/4 + 4 roundings of its exact value (q < 32).
+// Scattered table reads were the L1 limit of the pass; FP64 keeps exact
+// per-element look-ups.
+struct TwRun {
+  float2 a, s4, b1, b2, b3;
+  __device__ __forceinline__ static float2 look(const float2 *thi, const float2 *tlo, int h,
+                                                int hmask, long long mm) {
+    return cmul(thi[mm >> h], tlo[mm & hmask]);
+  }
+  __device__ __forceinline__ void init(const float2 *thi, const float2 *tlo, int h, int hmask,
+                                       long long jm, int r0, int tpf) {
+    b1 = look(thi, tlo, h, hmask, jm * tpf);
+    s4 = look(thi, tlo, h, hmask, jm * 4 * tpf);
+    a = look(thi, tlo, h, hmask, jm * r0);
+    b2 = cmul(b1, b1);
+    b3 = cmul(b2, b1);
+  }
+  // call with q = 0, 1, 2, ... (compile-time after unrolling)
+  __device__ __forceinline__ float2 next(int q) {
+    const int i = q & 3;
+    if (q > 0 && i == 0) a = cmul(a, s4);
+    return i == 0 ? a : cmul(a, i == 1 ? b1 : (i == 2 ? b2 : b3));
+  }
+};
 
 __device__ __forceinline__ double sq_sum(double2 v) { return __dadd_rn(__dmul_rn(v.x, v.x), __dmul_rn(v.y, v.y)); }
 __device__ __forceinline__ float sq_sum(float2 v) { return __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)); }
@@ -317,20 +419,30 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
         asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
         if (a.inverse || logNs > 0) {
           // each thread rewrites only the elements it loaded: no barrier needed here
+          TwRun tr;
+          if constexpr (sizeof(T) == 4)
+            if (logNs > 0)
+              tr.init(reinterpret_cast<const float2 *>(thi), reinterpret_cast<const float2 *>(tlo),
+                      a.tw_h, hmask, jm, r0, TPF);
 #pragma unroll
           for (int q = 0; q < ITER; q++) {
             V *p = dst + q * TPF + ((q * TPF) >> 4);
             V v = *p;
             if (a.inverse) v.y = -v.y;
             if (logNs > 0) {
-              const long long mm = mm0 + q * dmm;
-              v = cmul(v, cmul(thi[mm >> a.tw_h], tlo[mm & hmask]));
+              if constexpr (sizeof(T) == 4) {
+                v = cmul(v, tr.next(q));
+              } else {
+                const long long mm = mm0 + q * dmm;
+                v = cmul(v, cmul(thi[mm >> a.tw_h], tlo[mm & hmask]));
+              }
             }
             *p = v;
           }
         }
       } else {
         // row-group partials added on load (first pass after the streaming perm+filter)
+        // (a first pass: logNs = 0 in practice, so per-element look-ups stay)
         constexpr int LB = ITER < 4 ? ITER : 4;
 #pragma unroll
         for (int q0 = 0; q0 < ITER; q0 += LB) {
@@ -438,7 +550,8 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
     }
   }
   __syncthreads();
-  cta_fft<V, LOGR, G>(sm, twR);
+  if constexpr (LOGR <= 9) rt_cta_fft<V, LOGR, G>(sm, twR);
+  else cta_fft<V, LOGR, G>(sm, twR);
   V *__restrict__ out = reinterpret_cast<V *>(a.out);
   T *__restrict__ smp = reinterpret_cast<T *>(a.samples);
   const bool g_fast_out = logNs >= 0 && (1LL << logNs) >= G;
@@ -457,7 +570,7 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
                            ((long long)k0 << logNs);
       const long long ds = (long long)TPF << logNs;
       const V *sp = sm + g * RP + padded(k0);
-#pragma unroll
+#pragma unroll 4
       for (int q = 0; q < ITER; q++) {
         V v = sp[q * TPF + ((q * TPF) >> 4)];
         if (a.inverse) v.y = -v.y;
