@@ -4,7 +4,8 @@
 // Data layout in HBM (T = double in FP64 mode, float in MIXED mode):
 //   x            n complex T (caller)             signal
 //   filt         w complex T                      filter taps
-//   filt_bm      B x (w/B + 1) complex T          the taps bucket-major (streaming form)
+//   filt_bm      B x TT complex T                 the taps bucket-major (streaming form),
+//                                                TT = w/B + 1 rounded up to even
 //   hinv         n/B + 1 complex double           conj(H)/|H|^2 around bin 0
 //   rsamp        RLFC_loops x W_RLFC T            |FFT_W(restricted x)|^2
 //   J2b / J2     RLFC_loops x B_thresh int        RLFC blocks / merged ids

@@ -40,7 +40,8 @@ namespace gsfft {
 namespace {
 
 constexpr int ST = 128;      // B must be a multiple of this
-constexpr int NSTAGE = 3;    // shared-memory ring of tiles
+constexpr int NSTAGE = 3;    // shared-memory ring of tiles (taps read from L2)
+constexpr int NSTAGE_STG = 4; // ring of the staged-tap form (one CTA per SM)
 constexpr int MAXT = 32;     // full tiles of taps per bucket (w / B) supported
 constexpr int MAXL = 16;     // loops supported
 constexpr int PFD = 1;        // filter taps loaded ahead per thread
@@ -49,6 +50,11 @@ constexpr unsigned NONE = 0x7fffffffu;
 
 // columns per work item: one consumer thread per (column, loop)
 inline int cols_per_item(int loops) { return 64 * loops + 64 <= 1024 ? 64 : 32; }
+
+// taps per bucket in the bucket-major table: the w/B full-tile taps plus the
+// partial one, rounded up to even so that every bucket's row is a multiple of
+// 16 bytes (bulk copies)
+__host__ __device__ inline int taps_per_bucket(int tiles) { return (tiles + 2) & ~1; }
 
 struct HitTab {
   unsigned s[MAXL][MAXT];  // (row offset << 8) | j, sorted by row offset
@@ -66,6 +72,12 @@ __device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned coun
 
 __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
 }
 
 // The signal streams through L2 once; marking its tiles evict-first keeps the
@@ -91,6 +103,16 @@ __device__ __forceinline__ void tma_load_tile(void *dst, const CUtensorMap *tm, 
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
       " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x0), "r"(y0), "r"(smem_u32(bar)), "l"(pol)
+      : "memory");
+}
+
+// one bucket's taps (bytes: a multiple of 16) into this thread's slot
+__device__ __forceinline__ void bulk_load_taps(void *dst, const void *src, unsigned bytes,
+                                               unsigned long long *bar, unsigned long long pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1], %2, [%3], %4;" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
       : "memory");
 }
 
@@ -137,8 +159,8 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 //  * the last warp (RLFC loops only): copies the RLFC sub-samples out of
 //    each tile.
 // No block-wide barrier inside the stream.
-template <typename T, int CW, int MAXTH>
-__global__ void __launch_bounds__(MAXTH, MAXTH <= 640 ? CTAS_PER_SM : 1)
+template <typename T, int CW, int MAXTH, int NS, bool STG>
+__global__ void __launch_bounds__(MAXTH, (MAXTH <= 640 && !STG) ? CTAS_PER_SM : 1)
 pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V *__restrict__ filt,
               int logn, int logB, int w, int rt, int tiles, int rows_per_group, int groups, int L,
               Draws d, HitTab ht, typename Cx<T>::V *__restrict__ bins, int nrlfc, int logsig,
@@ -152,7 +174,8 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   // each loop's sorted list twice in a row, so a rotated walk needs no wrap
   __shared__ unsigned S2[MAXL][2 * MAXT];
   __shared__ unsigned s_a[MAXL], s_beta[MAXL], s_xrow[MAXL];
-  __shared__ __align__(8) unsigned long long full[NSTAGE], empty[NSTAGE];
+  __shared__ __align__(8) unsigned long long full[NS], empty[NS];
+  __shared__ __align__(8) unsigned long long tapbar[STG ? MAXTH / 32 : 1];
   __shared__ volatile int abort_flag;
   const int tid = threadIdx.x;
   const int B = 1 << logB;
@@ -160,7 +183,7 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   const int nb = 1 << lognb;
   const unsigned nbm = (unsigned)nb - 1u;
   const unsigned nmask = (1u << logn) - 1u;
-  const int TT = tiles + 1;  // taps per bucket in the bucket-major table
+  const int TT = taps_per_bucket(tiles);  // row length of the bucket-major table
   const unsigned stage_bytes = (unsigned)(rt * CW * sizeof(V));
   const int ntile = rows_per_group / rt;
   const int ncb = B / CW;
@@ -179,10 +202,12 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   }
   if (tid == 0) {
     abort_flag = 0;
-    for (int s = 0; s < NSTAGE; s++) {
+    for (int s = 0; s < NS; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], NREL);
     }
+    if (STG)
+      for (int i = 0; i < NCW; i++) mbar_init(&tapbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -199,9 +224,9 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
       const int cb = it % ncb, g = it / ncb;
       const int c0 = cb * CW;
       for (int t = 0; t < ntile; t++, k++) {
-        const int st = (int)(k % NSTAGE);
+        const int st = (int)(k % NS);
         const V *tl = tile0 + (size_t)st * rt * CW;
-        if (!mbar_wait(&full[st], (unsigned)((k / NSTAGE) & 1))) {
+        if (!mbar_wait(&full[st], (unsigned)((k / NS) & 1))) {
           abort_flag = 1;
           atomicExch(err, 1);
           return;
@@ -234,8 +259,8 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
       for (int it = blockIdx.x; it < items && ok; it += gridDim.x) {
         const int cb = it % ncb, g = it / ncb;
         for (int t = 0; t < ntile; t++, k++) {
-          const int st = (int)(k % NSTAGE);
-          if (!mbar_wait(&empty[st], (unsigned)((k / NSTAGE) & 1) ^ 1u) || abort_flag) {
+          const int st = (int)(k % NS);
+          if (!mbar_wait(&empty[st], (unsigned)((k / NS) & 1) ^ 1u) || abort_flag) {
             abort_flag = 1;
             ok = false;
             break;
@@ -246,8 +271,8 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
         }
       }
       // stay until the last load of every stage has landed (bounded)
-      for (long long j = k - NSTAGE < 0 ? 0 : k - NSTAGE; j < k; j++)
-        if (!mbar_wait(&full[j % NSTAGE], (unsigned)((j / NSTAGE) & 1))) {
+      for (long long j = k - NS < 0 ? 0 : k - NS; j < k; j++)
+        if (!mbar_wait(&full[j % NS], (unsigned)((j / NS) & 1))) {
           atomicExch(err, 1);
           break;
         }
@@ -262,6 +287,11 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
   const unsigned *S = S2[l];
   const unsigned long long keep = policy_evict_last();
   long long k = 0;
+  // staged form: this thread's slot of TT taps after the tile ring, and its
+  // warp's copy barrier
+  V *const tslot = reinterpret_cast<V *>(dsm + (size_t)NS * stage_bytes) + (size_t)tid * TT;
+  unsigned long long *const tbar = &tapbar[STG ? (tid >> 5) : 0];
+  unsigned tap_phase = 0;
   for (int it = blockIdx.x; it < items; it += gridDim.x) {
     const int cb = it % ncb, g = it / ncb;
     const int c0 = cb * CW;
@@ -274,6 +304,18 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     const int bl = (int)(prod & (unsigned)(B - 1));
     const unsigned q = (prod & nmask) >> logB;
     const unsigned sl = (0u - q * beta) & nbm;
+    const V *fcol = filt + (size_t)bl * TT;  // the bucket's taps, contiguous
+    if constexpr (STG) {
+      // One bulk copy of the bucket's taps into this thread's slot per item,
+      // completing on the warp's barrier.  At the first __syncwarp every lane
+      // is past its last read of the previous taps and its wait on the
+      // previous phase; the proxy fence orders those reads before the copy.
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive_expect(tbar, 32u * (unsigned)(TT * sizeof(V)));
+      __syncwarp();
+      bulk_load_taps(tslot, fcol, (unsigned)(TT * sizeof(V)), tbar, keep);
+    }
     // mw: first sorted entry with v >= nb - s (binary search)
     int lo = 0, hi = tiles;
     const unsigned lim = (unsigned)nb - sl;
@@ -295,30 +337,40 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
     }
     int mc = mw + lo;
     const int me = mw + tiles;
-    const V *fcol = filt + (size_t)bl * TT;  // the bucket's taps, contiguous
-    unsigned nm = NONE, er = NONE;
+    unsigned nm = NONE, er = NONE, ent = 0;
     // taps of the next PFD hits, loaded ahead (the last entries of the
     // doubled list are valid indices, so loading past me is harmless)
     V fv[PFD];
+    if constexpr (!STG) {
 #pragma unroll
-    for (int u = 0; u < PFD; u++)
-      fv[u] = ld_tap(fcol + (S[min(mc + u, 2 * tiles - 1)] & 255u), keep);
+      for (int u = 0; u < PFD; u++)
+        fv[u] = ld_tap(fcol + (S[min(mc + u, 2 * tiles - 1)] & 255u), keep);
+    }
     V fe = mk((T)0, (T)0);
     if (mc < me) {
-      const unsigned ent = S[mc];
+      ent = S[mc];
       nm = (ent >> 8) + sl - (mc < tiles ? (unsigned)nb : 0u);
     }
     if (bl < residue) {
       er = (xrow + sl) & nbm;
       if (er < (unsigned)rbeg) er = NONE;
-      else fe = ld_tap(fcol + tiles, keep);
+      else if constexpr (!STG) fe = ld_tap(fcol + tiles, keep);
+    }
+    if constexpr (STG) {
+      if (!mbar_wait(tbar, tap_phase)) {
+        abort_flag = 1;
+        atomicExch(err, 1);
+        return;
+      }
+      tap_phase ^= 1u;
+      if (er != NONE) fe = tslot[tiles];
     }
     T re = 0, im = 0;
 
     for (int t = 0; t < ntile; t++, k++) {
-      const int st = (int)(k % NSTAGE);
+      const int st = (int)(k % NS);
       const V *tl = tile0 + (size_t)st * rt * CW;
-      if (!mbar_wait(&full[st], (unsigned)((k / NSTAGE) & 1))) {
+      if (!mbar_wait(&full[st], (unsigned)((k / NS) & 1))) {
         abort_flag = 1;
         atomicExch(err, 1);
         return;
@@ -328,15 +380,26 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
       // falls in this tile
       while (nm < r1) {
         const V xv = tl[((nm - r0) << LOGCW) + col];
-        re = fma(xv.x, fv[0].x, re);
-        re = fma(-xv.y, fv[0].y, re);
-        im = fma(xv.x, fv[0].y, im);
-        im = fma(xv.y, fv[0].x, im);
-#pragma unroll
-        for (int u = 0; u + 1 < PFD; u++) fv[u] = fv[u + 1];
+        V f;
+        if constexpr (STG) f = tslot[ent & 255u];
+        else f = fv[0];
+        re = fma(xv.x, f.x, re);
+        re = fma(-xv.y, f.y, re);
+        im = fma(xv.x, f.y, im);
+        im = fma(xv.y, f.x, im);
         const int m = ++mc;
-        fv[PFD - 1] = ld_tap(fcol + (S[min(m + PFD - 1, 2 * tiles - 1)] & 255u), keep);
-        nm = m < me ? (S[m] >> 8) + sl - (m < tiles ? (unsigned)nb : 0u) : NONE;
+        if constexpr (STG) {
+          nm = NONE;
+          if (m < me) {
+            ent = S[m];
+            nm = (ent >> 8) + sl - (m < tiles ? (unsigned)nb : 0u);
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u + 1 < PFD; u++) fv[u] = fv[u + 1];
+          fv[PFD - 1] = ld_tap(fcol + (S[min(m + PFD - 1, 2 * tiles - 1)] & 255u), keep);
+          nm = m < me ? (S[m] >> 8) + sl - (m < tiles ? (unsigned)nb : 0u) : NONE;
+        }
       }
       if (er < r1) {
         const V xv = tl[((er - r0) << LOGCW) + col];
@@ -400,32 +463,47 @@ unsigned inv_odd(unsigned a) {  // a^-1 mod 2^32 for odd a (Newton)
   return x;
 }
 
-template <typename T, int CW, int MAXTH>
+// dynamic shared memory of one CTA: the tile ring, plus the consumers' tap
+// slots in the staged form
+inline int pf_smem_bytes(int es, int cw, int rt, int loops, int tiles, int ns, bool stg) {
+  return ns * rt * cw * es + (stg ? cw * loops * taps_per_bucket(tiles) * es : 0);
+}
+constexpr int PF_SMEM_LIMIT = 218 * 1024;  // dynamic bytes, leaving room for the static tables
+
+template <typename T, int CW, int MAXTH, int NS, bool STG>
 int launch_CW(const CUtensorMap &tm, const void *filt, int logn, int logB, int w, int rt, int tiles,
               int groups, int loops, const Draws &d, const HitTab &ht, void *bins, int nrlfc,
               int logsig, void *y, int W, int *err, cudaStream_t st) {
   typedef typename Cx<T>::V V;
   const int B = 1 << logB;
-  const int smem = NSTAGE * rt * CW * (int)sizeof(V);
+  const int smem = pf_smem_bytes((int)sizeof(V), CW, rt, loops, tiles, NS, STG);
   const int threads = CW * loops + (nrlfc > 0 ? 64 : 32);
   static int attr = 0;
   if (attr < smem) {
-    GS_CUDA(cudaFuncSetAttribute(pf_tma_kernel<T, CW, MAXTH>,
+    GS_CUDA(cudaFuncSetAttribute(pf_tma_kernel<T, CW, MAXTH, NS, STG>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr = smem;
   }
   int dev = 0, sms = 0, per_sm = 0;
   GS_CUDA(cudaGetDevice(&dev));
   GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pf_tma_kernel<T, CW, MAXTH>,
+  GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pf_tma_kernel<T, CW, MAXTH, NS, STG>,
                                                         threads, smem));
   const int items = (B / CW) * groups;
   const int grid = std::max(1, std::min(items, std::max(per_sm, 1) * sms));
   const int rows_per_group = (1 << (logn - logB)) / groups;
-  pf_tma_kernel<T, CW, MAXTH><<<grid, threads, smem, st>>>(
+  pf_tma_kernel<T, CW, MAXTH, NS, STG><<<grid, threads, smem, st>>>(
       tm, (const V *)filt, logn, logB, w, rt, tiles, rows_per_group, groups, loops, d, ht, (V *)bins,
       nrlfc, logsig, (V *)y, W, err);
   return GSFFT_OK;
+}
+
+// FP32 reads the taps from a per-thread shared-memory copy (one bulk copy per
+// work item) when the slots fit beside a ring of NSTAGE_STG tiles: a warp's
+// scattered 8-byte tap loads from L2 touched 32 cache lines each and were the
+// limit of the pass.
+inline bool pf_stream_staged(int cw, int rt, int loops, int tiles) {
+  return pf_smem_bytes(8, cw, rt, loops, tiles, NSTAGE_STG, true) <= PF_SMEM_LIMIT;
 }
 
 template <typename T>
@@ -434,25 +512,29 @@ int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int l
              int logsig, void *y, int W, int *err, cudaStream_t st) {
   const int cw = cols_per_item(loops);
   const bool small = cw * loops + (nrlfc > 0 ? 64 : 32) <= 640;
-#define GO(CWV, MT)                                                                                \
-  return launch_CW<T, CWV, MT>(tm, filt, logn, logB, w, rt, tiles, groups, loops, d, ht, bins, nrlfc, \
-                               logsig, y, W, err, st)
+#define GO(CWV, MT, NSV, STGV)                                                                     \
+  return launch_CW<T, CWV, MT, NSV, STGV>(tm, filt, logn, logB, w, rt, tiles, groups, loops, d, ht, \
+                                          bins, nrlfc, logsig, y, W, err, st)
   if (cw == 64) {
-    if (small) GO(64, 640);
-    GO(64, 1024);
+    if (small) {
+      if constexpr (sizeof(T) == 4)
+        if (pf_stream_staged(cw, rt, loops, tiles)) GO(64, 640, NSTAGE_STG, true);
+      GO(64, 640, NSTAGE, false);
+    }
+    GO(64, 1024, NSTAGE, false);
   }
-  if (small) GO(32, 640);
-  GO(32, 1024);
+  if (small) GO(32, 640, NSTAGE, false);
+  GO(32, 1024, NSTAGE, false);
 #undef GO
 }
 
 }  // namespace
 
-int stream_taps_count(int w, int B) { return B * (w / B + 1); }
+int stream_taps_count(int w, int B) { return B * taps_per_bucket(w / B); }
 
 int launch_stream_taps(int precision, const void *filt, int w, int B, void *taps_bm,
                        cudaStream_t st) {
-  const int TT = w / B + 1;
+  const int TT = taps_per_bucket(w / B);
   const long long cnt = (long long)B * TT;
   const unsigned grid = (unsigned)((cnt + 255) / 256);
   if (precision == GSFFT_FP64)

@@ -44,8 +44,9 @@ bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops);
 int stream_pf_groups(int n, int B, int loops, int precision);
 int launch_sum_partials(int precision, const void *part, int groups, long long count, void *out,
                         cudaStream_t st);
-// Bucket-major tap table of the streaming pass: taps_bm[b * (w/B + 1) + j] =
-// filt[j * B + b] (zero past w); stream_taps_count elements.
+// Bucket-major tap table of the streaming pass: taps_bm[b * TT + j] =
+// filt[j * B + b] (zero past w), TT = w/B + 1 rounded up to even (rows of a
+// multiple of 16 bytes); stream_taps_count elements.
 int stream_taps_count(int w, int B);
 int launch_stream_taps(int precision, const void *filt, int w, int B, void *taps_bm, cudaStream_t st);
 // filt here is the bucket-major table
