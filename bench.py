@@ -240,7 +240,7 @@ def useful_bytes(p, es):
 # captures summarised under profiles/ (keyed by kernel, form and workload):
 # profiles/pf_tma_kernel_stream_perm_filter.md.
 TRAFFIC = {
-    ("perm_filter", "stream", "q27k16000"): 1100303360 + 29271552,
+    ("perm_filter", "stream", "q27k16000"): 1099172352 + 28483584,
 }
 
 
