@@ -381,7 +381,7 @@ int gsfft_stage_perm_filter_stream(int precision, const void *d_x, int n,
   const bool fl = precision == GSFFT_MIXED;
   void *taps = nullptr, *part = nullptr, *tbm = nullptr;
   int *err = nullptr;
-  const int groups = stream_pf_groups(n, B, loops, precision);
+  const int groups = stream_pf_groups(n, B, w, loops, precision);
   const size_t es = fl ? sizeof(float2) : sizeof(double2);
   if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) return GSFFT_ERR_ALLOC;
   if (cudaMalloc(&part, es * (size_t)groups * loops * B) != cudaSuccess ||

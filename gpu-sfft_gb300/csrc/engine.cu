@@ -131,7 +131,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
                      (precision == GSFFT_MIXED && stream_bytes < gather_bytes));
   }
   if (P->use_stream) {
-    P->groups = stream_pf_groups(p.n, p.B, p.loops, precision);
+    P->groups = stream_pf_groups(p.n, p.B, p.w, p.loops, precision);
     A(ybuf, V * (size_t)p.RLFC_loops * p.W_RLFC);
     A(bpart, V * (size_t)P->groups * p.loops * p.B);
     A(filt_bm, V * (size_t)stream_taps_count(p.w, p.B));

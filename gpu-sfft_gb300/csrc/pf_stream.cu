@@ -569,16 +569,19 @@ static int stream_rows_per_tile(int n, int B, int precision) {
   return std::min(n / B, precision == GSFFT_FP64 ? 32 : 64);  // 32 KiB tiles of 64 columns
 }
 
-int stream_pf_groups(int n, int B, int loops, int precision) {
+int stream_pf_groups(int n, int B, int w, int loops, int precision) {
   const int nb = n / B;
   const int rt = stream_rows_per_tile(n, B, precision);
   int dev = 0, sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int cw = cols_per_item(loops);
+  // the staged FP32 form runs one CTA per SM (the dispatch's choice)
+  const bool stg = precision != GSFFT_FP64 && cw == 64 && 64 * loops + 64 <= 640 &&
+                   pf_stream_staged(cw, rt, loops, w / B);
   // enough work items (column block x row group) for ~6 per persistent CTA,
   // each item at least four tiles long
-  const long long want = 6LL * CTAS_PER_SM * sms;
-  const int cw = cols_per_item(loops);
+  const long long want = 6LL * (stg ? 1 : CTAS_PER_SM) * sms;
   int groups = 1;
   while ((long long)(B / cw) * groups < want && nb / (groups * 2) >= 4 * rt) groups *= 2;
   return groups;
@@ -610,7 +613,7 @@ int launch_perm_filter_stream(int precision, const void *x, int n, const void *f
   const bool dbl = precision == GSFFT_FP64;
   const int es = dbl ? 16 : 8;
   const int rt = stream_rows_per_tile(n, B, precision);
-  const int groups = stream_pf_groups(n, B, loops, precision);
+  const int groups = stream_pf_groups(n, B, w, loops, precision);
   const int cw = cols_per_item(loops);
   CUtensorMap tm;
   const cuuint64_t gdim[2] = {(cuuint64_t)B * (es / 8), (cuuint64_t)nb};

@@ -41,7 +41,7 @@ int launch_perm_filter(int precision, const void *x, int n, const void *filt, in
 bool stream_pf_supported(int n, int B, int loops, int W, int RLFC_loops);
 // Row groups of the streaming pass: it writes `groups` partial bin arrays
 // (groups x loops x B), to be added in group order.
-int stream_pf_groups(int n, int B, int loops, int precision);
+int stream_pf_groups(int n, int B, int w, int loops, int precision);
 int launch_sum_partials(int precision, const void *part, int groups, long long count, void *out,
                         cudaStream_t st);
 // Bucket-major tap table of the streaming pass: taps_bm[b * TT + j] =

@@ -271,28 +271,34 @@ vote_count_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, unsigned
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
   if (lane == 0 && t < w.Bt) cnt[t] = (int)c;
   const unsigned s = blk_sum(lane == 0 ? c : 0u, ws);
-  if (threadIdx.x == 0) blk[blockIdx.x] = (int)s;
-  // last block: exclusive scan of the block counts
-  __threadfence();
-  __syncthreads();
+  // last block: exclusive scan of the block counts.  Only the block count has
+  // to be visible to it, so only thread 0 fences (a fence in every thread
+  // would wait for that thread's vote-table writes to reach memory).
   if (threadIdx.x == 0) {
+    blk[blockIdx.x] = (int)s;
+    __threadfence();
     const unsigned tk = atomicAdd(&ctl->ticket, 1u);
     is_last = tk == gridDim.x - 1;
   }
   __syncthreads();
   if (!is_last) return;
   __threadfence();
-  unsigned run = 0;
-  for (int c0 = 0; c0 < (int)gridDim.x; c0 += VT) {
-    const int i = c0 + threadIdx.x;
-    const unsigned v = i < (int)gridDim.x ? (unsigned)atomicAdd(&blk[i], 0) : 0u;
-    unsigned tot;
-    const unsigned e = blk_excl_scan(v, ws, &tot);
-    if (i < (int)gridDim.x) blk_pre[i] = (int)(run + e);
-    run += tot;
+  // Each thread scans a contiguous run of block counts: all its L2 loads are
+  // independent, then one block scan (the serial tail used to pay an L2 round
+  // trip and three barriers per 256 counts).
+  const int nblk = (int)gridDim.x;
+  const int per = (nblk + VT - 1) / VT;
+  const int i0 = min(nblk, (int)threadIdx.x * per), i1 = min(nblk, i0 + per);
+  unsigned sum = 0;
+  for (int i = i0; i < i1; i++) sum += (unsigned)__ldcg(&blk[i]);
+  unsigned tot;
+  unsigned run = blk_excl_scan(sum, ws, &tot);
+  for (int i = i0; i < i1; i++) {
+    blk_pre[i] = (int)run;
+    run += (unsigned)__ldcg(&blk[i]);
   }
   if (threadIdx.x == 0) {
-    blk_pre[gridDim.x] = (int)run;
+    blk_pre[nblk] = (int)tot;
     ctl->ticket = 0;
   }
 }
@@ -380,9 +386,11 @@ vote_write_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, const un
       next += ctot;
     });
   }
-  __threadfence();
+  // the last block to finish publishes the new candidate count; every block
+  // read the old one before its thread 0 takes a ticket (barrier + fence)
   __syncthreads();
   if (threadIdx.x == 0) {
+    __threadfence();
     const unsigned tk = atomicAdd(&ctl->ticket, 1u);
     is_last = tk == gridDim.x - 1;
   }
