@@ -367,6 +367,10 @@ constexpr int CHUNK_MIN = 2048; // smallest chunk per CTA
 constexpr int UN = 8;           // loads in flight per thread in the scan passes
 constexpr int COOP_SMEM = (CT / 32) * (HIST_BINS / 2) * 4;  // per-warp histograms
 constexpr long long MAX_CHUNK = 16LL * 65535;  // keeps a warp's 16-bit counters exact
+// CTAs per SM the register budget is set for: three for 32-bit keys (the
+// large scans need the memory parallelism; two measured slower), two for
+// 64-bit keys (no spills; the top-k rows are short).
+template <typename K> constexpr int coop_ctas_per_sm() { return sizeof(K) == 4 ? 3 : 2; }
 
 struct CoopArgs {
   const void *keys;
@@ -414,13 +418,14 @@ __device__ __forceinline__ unsigned ct_excl_scan(unsigned v, unsigned *ws, unsig
 }
 
 template <typename K>
-__global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
+__global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(CoopArgs a) {
   cg::grid_group grid = cg::this_grid();
   // one private histogram per warp, two 16-bit counters per word, so warps
   // never contend on a bin (a warp counts at most chunk / 16 < 65536 keys)
   extern __shared__ unsigned wh[];  // [CT / 32][HIST_BINS / 2]
   __shared__ unsigned ws[CT / 32];
   __shared__ unsigned long long s_prefix;
+  __shared__ unsigned s_settled[MAXB];  // per row: its rank falls among its floored zeros
   __shared__ long long s_rank;
   __shared__ unsigned s_bincount;
   const int tid = threadIdx.x, lane = tid & 31;
@@ -436,16 +441,17 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
     sz = dv < a.size ? dv : a.size;
     if (sz < 0) sz = 0;
   }
-  K floor = 0;
-  if (a.row_max && a.floor_rel > 0.0) {
+  // rounding floor of row r (0: none)
+  auto row_floor = [&](int r) -> K {
+    if (!(a.row_max && a.floor_rel > 0.0)) return (K)0;
     if (kb == 64) {
-      const double m = __longlong_as_double((long long)reinterpret_cast<const unsigned long long *>(a.row_max)[b]);
-      floor = (K)(unsigned long long)__double_as_longlong(m * a.floor_rel);
-    } else {
-      const float m = __uint_as_float(reinterpret_cast<const unsigned *>(a.row_max)[b]);
-      floor = (K)__float_as_uint((float)((double)m * a.floor_rel));
+      const double m = __longlong_as_double((long long)reinterpret_cast<const unsigned long long *>(a.row_max)[r]);
+      return (K)(unsigned long long)__double_as_longlong(m * a.floor_rel);
     }
-  }
+    const float m = __uint_as_float(reinterpret_cast<const unsigned *>(a.row_max)[r]);
+    return (K)__float_as_uint((float)((double)m * a.floor_rel));
+  };
+  const K floor = row_floor(b);
   const bool take_all = sz <= a.num;
   const long long chunk = ((sz + a.cpr - 1) / a.cpr + 31) & ~31LL;
   const long long lo = (long long)ci * chunk < sz ? (long long)ci * chunk : sz;
@@ -456,6 +462,8 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
   int cmp_shift = 0;  // low bits ignored by the final comparisons
   bool done = take_all;
   bool counted = false;  // the chunk counts for the final threshold are already stored
+  // every row settled: grid-uniform, so every CTA skips the same grid syncs
+  bool all_done = take_all;
   // (grid-uniform condition: every CTA reaches the same grid syncs)
   if (a.row_max && a.floor_rel > 0.0) {
     const bool mine_row = !take_all && floor != 0;
@@ -489,14 +497,22 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
       atomicAdd(&a.zero_count[b], tz);
     }
     grid.sync();
-    const long long zrow = (long long)__ldcg(&a.zero_count[b]);
-    if (mine_row && zrow > rank) {  // ascending rank `rank` is a zero
+    // Every row's zero count is visible here and no longer changes, so every
+    // CTA reaches the same verdicts.  One thread per row loads them (every
+    // thread of every CTA loading the same words made an L2 hot spot).
+    if (tid < a.batch)
+      s_settled[tid] = !take_all && row_floor(tid) != 0 && (long long)__ldcg(&a.zero_count[tid]) > rank;
+    __syncthreads();
+    if (s_settled[b]) {  // ascending rank `rank` is a zero
       done = true;
       counted = true;
     }
+    bool all = !take_all;
+    for (int r = 0; r < a.batch; r++) all = all && s_settled[r];
+    all_done = all_done || all;
   }
   int shift = kb;
-  for (int p = 0; p < npass; p++) {
+  for (int p = 0; p < npass && !all_done; p++) {
     const int width = kb == 64 ? w64[p] : w32[p];
     shift -= width;
     if (!done) {
@@ -550,13 +566,12 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
       // the digit holding ascending rank `rank` of this row
       const unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
       constexpr int per = HIST_BINS / CT;
-      unsigned local[per];
-      unsigned sum = 0;
-#pragma unroll
-      for (int q = 0; q < per; q++) {
-        local[q] = __ldcg(&gh[tid * per + q]);
-        sum += local[q];
-      }
+      static_assert(per == 4, "one 16-byte histogram load per thread");
+      // every CTA of the row reads these words: one 16-byte load per thread
+      // keeps the requests per L2 line down
+      const uint4 h4 = __ldcg(reinterpret_cast<const uint4 *>(gh) + tid);
+      const unsigned local[per] = {h4.x, h4.y, h4.z, h4.w};
+      const unsigned sum = h4.x + h4.y + h4.z + h4.w;
       unsigned tot;
       const unsigned before = ct_excl_scan(sum, ws, &tot);
       unsigned run = before;
@@ -582,6 +597,7 @@ __global__ void __launch_bounds__(CT) sel_coop_kernel(CoopArgs a) {
         done = true;  // every key of the bin was floored to exactly 0
       }
       if (p == npass - 1) done = true;
+      if (a.batch == 1) all_done = done;  // one row: its state is the grid's
     }
   }
   // counting pass: (#greater, #equal) of this chunk
@@ -693,6 +709,7 @@ int coop_grid() {
                              COOP_SMEM) != cudaSuccess)
       return -1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K>, CT, COOP_SMEM);
+    if (per > coop_ctas_per_sm<K>()) per = coop_ctas_per_sm<K>();
     g = per > 0 ? per * sms : -1;
   }
   return g;
