@@ -34,11 +34,21 @@ __global__ void convert_taps_kernel(const double2 *__restrict__ src, void *dst, 
 
 // First kernel of every run: clears the run state and the row maxima and
 // advances the device epoch (a graph replay of the run advances it too).
-__global__ void run_begin_kernel(RunCtl *ctl, unsigned long long *rmax, int nrmax, unsigned *epoch) {
-  int *c = reinterpret_cast<int *>(ctl);
-  for (int i = threadIdx.x; i < (int)(sizeof(RunCtl) / sizeof(int)); i += blockDim.x) c[i] = 0;
-  for (int i = threadIdx.x; i < nrmax; i += blockDim.x) rmax[i] = 0ull;
-  if (threadIdx.x == 0) *epoch = *epoch + 1u;
+// First kernel of a run (launched normally, after everything before it):
+// block 0 clears the control block and the row maxima and advances the epoch;
+// every block zeroes part of the residue bitmaps F_l.
+__global__ void run_begin_kernel(RunCtl *ctl, unsigned long long *rmax, int nrmax, unsigned *epoch,
+                                 unsigned *bm, long long bm_words) {
+  pdl_enter();
+  if (blockIdx.x == 0) {
+    int *c = reinterpret_cast<int *>(ctl);
+    for (int i = threadIdx.x; i < (int)(sizeof(RunCtl) / sizeof(int)); i += blockDim.x) c[i] = 0;
+    for (int i = threadIdx.x; i < nrmax; i += blockDim.x) rmax[i] = 0ull;
+    if (threadIdx.x == 0) *epoch = *epoch + 1u;
+  }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < bm_words;
+       i += (long long)gridDim.x * blockDim.x)
+    bm[i] = 0u;
 }
 
 // hinv[idx] = conj(H)/|H|^2 with H = filter_freq[(n - d) mod n], d = idx - nb/2
@@ -239,8 +249,8 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   }
   if (!capturing) GS_CHECK(plan_epoch_advance(P, st));
   const int kb = P->precision == GSFFT_FP64 ? 8 : 4;
-  run_begin_kernel<<<1, 64, 0, st>>>(P->ctl, (unsigned long long *)P->rmax, p.RLFC_loops + p.loops,
-                                     P->d_epoch);
+  run_begin_kernel<<<128, 256, 0, st>>>(P->ctl, (unsigned long long *)P->rmax, p.RLFC_loops + p.loops,
+                                        P->d_epoch, P->bm_sig, (long long)(p.W_RLFC / 32) * p.loops_loc);
   GS_LAUNCHED();
   void *rmax_w = P->rmax;  // RLFC rows, then bucket rows (u64 in FP64, u32 in FP32)
   void *rmax_b = (char *)P->rmax + (size_t)kb * p.RLFC_loops;

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(ET)
 estimate_kernel_fixed(const int *__restrict__ cand, const RunCtl *ctl, int cap,
                       const typename Cx<T>::V *__restrict__ bins, unsigned nmask, int lognb, int B,
                       Draws d, const double2 *__restrict__ hinv, DevNode *nodes, double *mag2) {
+  pdl_enter();
   const int count = min(ctl->cand_count, cap);
   const int nb = 1 << lognb;
   for (int i = blockIdx.x * ET + threadIdx.x; i < count; i += gridDim.x * ET) {
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(ET)
 estimate_kernel(const int *__restrict__ cand, const RunCtl *ctl, int cap,
                 const typename Cx<T>::V *__restrict__ bins, int loops, unsigned nmask, int lognb,
                 int B, Draws d, const double2 *__restrict__ hinv, DevNode *nodes, double *mag2) {
+  pdl_enter();
   const int i = blockIdx.x * ET + threadIdx.x;
   const int count = min(ctl->cand_count, cap);
   if (i >= count) return;
@@ -136,6 +138,7 @@ estimate_kernel(const int *__restrict__ cand, const RunCtl *ctl, int cap,
 
 __global__ void gather_nodes_kernel(const DevNode *__restrict__ nodes, const int *__restrict__ idx,
                                     const int *count, int cap, DevNode *out) {
+  pdl_enter();
   const int k = blockIdx.x * 256 + threadIdx.x;
   if (k < min(*count, cap)) out[k] = nodes[idx[k]];
 }
@@ -150,14 +153,14 @@ int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, 
   const unsigned nmask = (unsigned)n - 1u;
   if (loops >= 2 && loops <= 16) {
     const int grid = min((cap + ET - 1) / ET, 152 * 8);
-#define EST_CASE(LL)                                                                            \
-  case LL:                                                                                      \
-    if (precision == GSFFT_FP64)                                                                \
-      estimate_kernel_fixed<double, LL><<<grid, ET, 0, st>>>(cand, ctl, cap, (const double2 *)bins, \
-                                                             nmask, lognb, B, d, hinv, nodes, mag2); \
-    else                                                                                        \
-      estimate_kernel_fixed<float, LL><<<grid, ET, 0, st>>>(cand, ctl, cap, (const float2 *)bins,   \
-                                                            nmask, lognb, B, d, hinv, nodes, mag2);  \
+#define EST_CASE(LL)                                                                              \
+  case LL:                                                                                        \
+    if (precision == GSFFT_FP64)                                                                  \
+      GS_CUDA(launch_pdl(estimate_kernel_fixed<double, LL>, dim3(grid), dim3(ET), 0, st, cand, ctl, \
+                         cap, (const double2 *)bins, nmask, lognb, B, d, hinv, nodes, mag2));       \
+    else                                                                                          \
+      GS_CUDA(launch_pdl(estimate_kernel_fixed<float, LL>, dim3(grid), dim3(ET), 0, st, cand, ctl,  \
+                         cap, (const float2 *)bins, nmask, lognb, B, d, hinv, nodes, mag2));        \
     break;
     switch (loops) {
       EST_CASE(2) EST_CASE(3) EST_CASE(4) EST_CASE(5) EST_CASE(6) EST_CASE(7) EST_CASE(8)
@@ -182,7 +185,8 @@ int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, 
 
 int launch_gather_nodes(const DevNode *nodes, const int *idx, const int *count, int cap,
                         DevNode *out, cudaStream_t st) {
-  gather_nodes_kernel<<<(cap + 255) / 256, 256, 0, st>>>(nodes, idx, count, cap, out);
+  GS_CUDA(launch_pdl(gather_nodes_kernel, dim3((cap + 255) / 256), dim3(256), 0, st, nodes, idx, count,
+                     cap, out));
   GS_LAUNCHED();
   return GSFFT_OK;
 }

@@ -367,6 +367,7 @@ __device__ __forceinline__ void row_max_update(void *rm, long long b, float v) {
 
 template <typename T, int LOGR>
 __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
+  pdl_enter();
   typedef typename Cx<T>::V V;
   constexpr int R = 1 << LOGR, G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), RP = rowpitch<T>(LOGR);
   constexpr int ITER = R * G / NT;  // elements per thread in the load / store phases
@@ -630,7 +631,7 @@ int launch_pass(const PassArgs &a, long long total_sub, cudaStream_t st) {
   }
   long long grid = (total_sub + G - 1) / G;
   if (grid > 0x7fffffffLL) return GSFFT_ERR_UNSUPPORTED;
-  fft_pass_kernel<T, LOGR><<<(unsigned)grid, NT, SM, st>>>(a);
+  GS_CUDA(launch_pdl(fft_pass_kernel<T, LOGR>, dim3((unsigned)grid), dim3(NT), SM, st, a));
   GS_LAUNCHED();
   return GSFFT_OK;
 }

@@ -41,6 +41,37 @@ extern thread_local int g_launch_counter;
     }                                                                         \
   } while (0)
 
+// ---------------------------------------------------------------- launches
+// Programmatic dependent launch.  The kernels of a run begin with pdl_enter():
+// griddepcontrol.wait returns once the preceding grid of the stream has
+// completed and its writes are visible (at once when the kernel was launched
+// normally), then launch_dependents lets the next kernel be scheduled as soon
+// as every block of this grid has passed its wait.  So only the launch of the
+// next kernel overlaps this one; its blocks wait before touching memory, and a
+// waiting grid never holds resources its predecessor still needs (all of the
+// predecessor's blocks have started by then).
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch `kernel` as a programmatic dependent of the stream's previous kernel.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ---------------------------------------------------------------- complex
 template <typename T> struct Cx;
 template <> struct Cx<double> { typedef double2 V; };

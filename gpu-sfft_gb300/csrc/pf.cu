@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(PF_THREADS)
 pf_kernel(const typename Cx<T>::V *__restrict__ x, unsigned nmask,
           const typename Cx<T>::V *__restrict__ filt, int w, int B, int loops, int per, Draws d,
           int quirk, typename Cx<T>::V *__restrict__ bins) {
+  pdl_enter();
   typedef typename Cx<T>::V V;
   const int b = blockIdx.x * PF_THREADS + threadIdx.x;
   if (b >= B) return;
@@ -74,13 +75,13 @@ int launch_perm_filter(int precision, const void *x, int n, const void *filt, in
   dim3 grid((B + PF_THREADS - 1) / PF_THREADS, chunks);
   const unsigned nmask = (unsigned)n - 1u;
   if (precision == GSFFT_FP64)
-    pf_kernel<double><<<grid, PF_THREADS, 0, st>>>((const double2 *)x, nmask, (const double2 *)filt,
-                                                   w, B, loops, per, d, quirk_residue ? 1 : 0,
-                                                   (double2 *)bins);
+    GS_CUDA(launch_pdl(pf_kernel<double>, grid, dim3(PF_THREADS), 0, st, (const double2 *)x, nmask,
+                       (const double2 *)filt, w, B, loops, per, d, quirk_residue ? 1 : 0,
+                       (double2 *)bins));
   else
-    pf_kernel<float><<<grid, PF_THREADS, 0, st>>>((const float2 *)x, nmask, (const float2 *)filt, w,
-                                                  B, loops, per, d, quirk_residue ? 1 : 0,
-                                                  (float2 *)bins);
+    GS_CUDA(launch_pdl(pf_kernel<float>, grid, dim3(PF_THREADS), 0, st, (const float2 *)x, nmask,
+                       (const float2 *)filt, w, B, loops, per, d, quirk_residue ? 1 : 0,
+                       (float2 *)bins));
   GS_LAUNCHED();
   return GSFFT_OK;
 }

@@ -165,6 +165,7 @@ pf_tma_kernel(const __grid_constant__ CUtensorMap tmap, const typename Cx<T>::V 
               int logn, int logB, int w, int rt, int tiles, int rows_per_group, int groups, int L,
               Draws d, HitTab ht, typename Cx<T>::V *__restrict__ bins, int nrlfc, int logsig,
               typename Cx<T>::V *__restrict__ y, int W, int *err) {
+  pdl_enter();
   typedef typename Cx<T>::V V;
   constexpr int LOGCW = CW == 64 ? 6 : 5;
   const int NCT = CW * L;  // consumer threads
@@ -492,9 +493,9 @@ int launch_CW(const CUtensorMap &tm, const void *filt, int logn, int logB, int w
   const int items = (B / CW) * groups;
   const int grid = std::max(1, std::min(items, std::max(per_sm, 1) * sms));
   const int rows_per_group = (1 << (logn - logB)) / groups;
-  pf_tma_kernel<T, CW, MAXTH, NS, STG><<<grid, threads, smem, st>>>(
-      tm, (const V *)filt, logn, logB, w, rt, tiles, rows_per_group, groups, loops, d, ht, (V *)bins,
-      nrlfc, logsig, (V *)y, W, err);
+  GS_CUDA(launch_pdl(pf_tma_kernel<T, CW, MAXTH, NS, STG>, dim3(grid), dim3(threads), smem, st, tm,
+                     (const V *)filt, logn, logB, w, rt, tiles, rows_per_group, groups, loops, d, ht,
+                     (V *)bins, nrlfc, logsig, (V *)y, W, err));
   return GSFFT_OK;
 }
 

@@ -64,7 +64,7 @@ int launch_sigma_bitmaps(const int *J2, const RunCtl *ctl_num, int max_num, int 
                          const Draws &d, unsigned *bitmaps, RunCtl *ctl, cudaStream_t st);
 
 // The same bitmaps and fmax_l straight from the RLFC blocks (total ids, with
-// duplicates); ctl->fmax must be zero on entry.
+// duplicates); the bitmaps and ctl->fmax must be zero on entry.
 int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, const Draws &d,
                              unsigned *bitmaps, RunCtl *ctl, cudaStream_t st);
 

@@ -134,6 +134,7 @@ __global__ void sigma_bits_kernel(const int *__restrict__ J2, const int *num_dev
 __global__ void sigma_from_blocks_kernel(const int *__restrict__ J2b, int total, int W, Draws d,
                                          int loops_loc, unsigned *bms, int words_per_map,
                                          int *fmax) {
+  pdl_enter();
   const int m = blockIdx.x * VT + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool ok = m < total;
@@ -230,6 +231,7 @@ constexpr int WPB = VT / 32;  // buckets (warps) per block
 __global__ void __launch_bounds__(VT)
 vote_count_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, unsigned *vote, int *cnt,
                   int *blk, int *blk_pre, RunCtl *ctl) {
+  pdl_enter();
   const unsigned epoch = *epoch_p;
   __shared__ unsigned ws[VT / 32];
   __shared__ int is_last;
@@ -307,6 +309,7 @@ vote_count_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, unsigned
 // the threshold: they only record their votes.
 __global__ void __launch_bounds__(VT)
 vote_mark_kernel(WalkArgs w, const unsigned *epoch_p, unsigned *vote) {
+  pdl_enter();
   const unsigned epoch = *epoch_p;
   const int warp = threadIdx.x >> 5;
   const int t = blockIdx.x * WPB + warp;
@@ -342,6 +345,7 @@ __global__ void __launch_bounds__(VT)
 vote_write_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, const unsigned *__restrict__ vote,
                   const int *__restrict__ cnt, const int *__restrict__ blk_pre, int nblk, int *cand,
                   int cap, RunCtl *ctl) {
+  pdl_enter();
   __shared__ unsigned ws[VT / 32];
   __shared__ int is_last;
   const int base_prev = ctl->cand_count;
@@ -434,10 +438,10 @@ int launch_sigma_bitmaps(const int *J2, const RunCtl *ctl_num, int max_num, int 
 int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, const Draws &d,
                              unsigned *bitmaps, RunCtl *ctl, cudaStream_t st) {
   const int words = W / 32;
-  GS_CUDA(cudaMemsetAsync(bitmaps, 0, sizeof(unsigned) * (size_t)words * loops_loc, st));
-  // ctl->fmax starts at 0 (the run clears RunCtl); every F_l is non-empty
-  sigma_from_blocks_kernel<<<(total + VT - 1) / VT, VT, 0, st>>>(J2b, total, W, d, loops_loc,
-                                                                  bitmaps, words, ctl->fmax);
+  // the bitmaps are zero on entry and ctl->fmax starts at 0 (the run's first
+  // kernel clears both); every F_l is non-empty
+  GS_CUDA(launch_pdl(sigma_from_blocks_kernel, dim3((total + VT - 1) / VT), dim3(VT), 0, st, J2b,
+                     total, W, d, loops_loc, bitmaps, words, (int *)ctl->fmax));
   GS_LAUNCHED();
   return GSFFT_OK;
 }
@@ -457,16 +461,17 @@ int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
   w.a = (unsigned)d.a[l];
   const int grid = (B_thresh + WPB - 1) / WPB;
   if (!may_complete) {
-    vote_mark_kernel<<<grid, VT, 0, st>>>(w, epoch, vote);
+    GS_CUDA(launch_pdl(vote_mark_kernel, dim3(grid), dim3(VT), 0, st, w, epoch, vote));
     GS_LAUNCHED();
     return GSFFT_OK;
   }
   int *blk_pre = blk + grid + 1;  // blk holds 2 * (grid + 1) ints
-  vote_count_kernel<<<grid, VT, 0, st>>>(w, epoch, (unsigned)loops_thresh, vote, cnt, blk, blk_pre,
-                                         ctl);
+  GS_CUDA(launch_pdl(vote_count_kernel, dim3(grid), dim3(VT), 0, st, w, epoch, (unsigned)loops_thresh,
+                     vote, cnt, blk, blk_pre, ctl));
   GS_LAUNCHED();
-  vote_write_kernel<<<grid, VT, 0, st>>>(w, epoch, (unsigned)loops_thresh, vote, cnt, blk_pre, grid,
-                                         cand, cap, ctl);
+  GS_CUDA(launch_pdl(vote_write_kernel, dim3(grid), dim3(VT), 0, st, w, epoch, (unsigned)loops_thresh,
+                     (const unsigned *)vote, (const int *)cnt, (const int *)blk_pre, grid, cand, cap,
+                     ctl));
   GS_LAUNCHED();
   return GSFFT_OK;
 }
