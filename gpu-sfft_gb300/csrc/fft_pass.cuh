@@ -149,6 +149,54 @@ template <typename T> __host__ __device__ constexpr int smem_of(int logr) {
          (tw_in_smem<T>(logr) ? (1 << logr) * (int)sizeof(typename Cx<T>::V) : 0);
 }
 
+// Inter-pass twiddles folded into the first shared-memory stage (FP32 passes
+// after the first): the stage's inputs are conjugated (inverse) and
+// multiplied by W^(jm r) in registers instead of in a separate read-modify-
+// write of shared memory.  Element r = t + e NB of the row takes
+//   W^(jm t) (W^(4 jm NB))^a (W^(jm NB))^b,  e = 4a + b,
+// from three two-level table look-ups per thread and running products (at
+// most about eight roundings).
+struct PreTw {
+  const float2 *thi, *tlo;
+  int h, hmask;
+  long long u0, Smask, Nsmask;
+  int inverse;
+  bool on;
+};
+
+__device__ __forceinline__ float2 tw_look(const PreTw &pt, long long mm) {
+  return cmul(__ldg(&pt.thi[mm >> pt.h]), __ldg(&pt.tlo[mm & pt.hmask]));
+}
+
+template <typename V, int E, int Q, int NB, int TPF>
+__device__ __forceinline__ void apply_pretw(V (&v)[Q][E], const PreTw &pt, int g, int t0) {
+  if constexpr (sizeof(decltype(V().x)) == 4) {
+    if (!pt.on) return;
+    const long long jm = ((pt.u0 + g) & pt.Smask) & pt.Nsmask;
+    const float2 s1 = tw_look(pt, jm * NB);
+    float2 s4 = make_float2(1.f, 0.f);
+    if constexpr (E >= 8) s4 = tw_look(pt, jm * 4 * NB);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      float2 wa = tw_look(pt, jm * (t0 + q * TPF)), w = wa;
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        if (e > 0) {
+          if ((e & 3) == 0) {
+            wa = cmul(wa, s4);
+            w = wa;
+          } else {
+            w = cmul(w, s1);
+          }
+        }
+        V x = v[q][e];
+        if (pt.inverse) x.y = -x.y;
+        v[q][e] = cmul(x, w);
+      }
+    }
+  }
+}
+
 // One Stockham stage of radix E inside shared memory, for all G rows, after
 // stages whose radices multiply to Ns = 2^LOGNS.  All strides are compile-time
 // constants: with padded(i) = i + i/16, NB = R/E and t < NB,
@@ -157,7 +205,7 @@ template <typename T> __host__ __device__ constexpr int smem_of(int logr) {
 // (k < Ns, powers of two), so every shared-memory access of a butterfly is one
 // base address plus an immediate offset.
 template <typename V, int LOGR, int G, int E, int LOGNS>
-__device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR) {
+__device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR, const PreTw &pt) {
   constexpr int R = 1 << LOGR;
   constexpr int RP = rowpitch<decltype(V().x)>(LOGR);
   constexpr int NT = imin((R / 16) * G, 512);
@@ -170,12 +218,25 @@ __device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR) {
   const int g = threadIdx.x / TPF, t0 = threadIdx.x % TPF;
   V *s = sm + g * RP;
   V v[Q][E];
+  // a first stage with folded inter-pass twiddles loads all its inputs first
+  const bool fold = LOGNS == 0 && pt.on;
+  if (fold) {
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      const V *rp = s + padded(t0 + q * TPF);
+#pragma unroll
+      for (int e = 0; e < E; e++) v[q][e] = rp[e * NB + ((e * NB) >> 4)];
+    }
+    apply_pretw<V, E, Q, NB, TPF>(v, pt, g, t0);
+  }
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     const int t = t0 + q * TPF;
-    const V *rp = s + padded(t);
+    if (!fold) {
+      const V *rp = s + padded(t);
 #pragma unroll
-    for (int e = 0; e < E; e++) v[q][e] = rp[e * NB + ((e * NB) >> 4)];
+      for (int e = 0; e < E; e++) v[q][e] = rp[e * NB + ((e * NB) >> 4)];
+    }
     if constexpr (LOGNS > 0) {
       const int k = t & (Ns - 1);
       if constexpr (sizeof(v[0][0].x) == 8 || E < 4) {
@@ -291,20 +352,20 @@ __device__ __forceinline__ void rt_cta_fft(V *sm, const V *__restrict__ twR) {
 }
 
 template <typename V, int LOGR, int G, int LOGNS>
-__device__ __forceinline__ void radix16_stages(V *sm, const V *__restrict__ twR) {
+__device__ __forceinline__ void radix16_stages(V *sm, const V *__restrict__ twR, const PreTw &pt) {
   if constexpr (LOGNS + 4 <= LOGR) {
-    smem_stage<V, LOGR, G, 16, LOGNS>(sm, twR);
-    radix16_stages<V, LOGR, G, LOGNS + 4>(sm, twR);
+    smem_stage<V, LOGR, G, 16, LOGNS>(sm, twR, pt);
+    radix16_stages<V, LOGR, G, LOGNS + 4>(sm, twR, pt);
   }
 }
 
 template <typename V, int LOGR, int G>
-__device__ __forceinline__ void cta_fft(V *sm, const V *__restrict__ twR) {
+__device__ __forceinline__ void cta_fft(V *sm, const V *__restrict__ twR, const PreTw &pt) {
   constexpr int LEFT = LOGR % 4;
-  if constexpr (LEFT == 1) smem_stage<V, LOGR, G, 2, 0>(sm, twR);
-  if constexpr (LEFT == 2) smem_stage<V, LOGR, G, 4, 0>(sm, twR);
-  if constexpr (LEFT == 3) smem_stage<V, LOGR, G, 8, 0>(sm, twR);
-  radix16_stages<V, LOGR, G, LEFT>(sm, twR);
+  if constexpr (LEFT == 1) smem_stage<V, LOGR, G, 2, 0>(sm, twR, pt);
+  if constexpr (LEFT == 2) smem_stage<V, LOGR, G, 4, 0>(sm, twR, pt);
+  if constexpr (LEFT == 3) smem_stage<V, LOGR, G, 8, 0>(sm, twR, pt);
+  radix16_stages<V, LOGR, G, LEFT>(sm, twR, pt);
 }
 
 // FP32 inter-pass twiddles W^(jm r), r = r0 + q TPF, q = 0, 1, ... in order,
@@ -397,6 +458,20 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
   // offsets padded(r) = padded(tid/G) + q TPF + q TPF/16 are compile-time.
   constexpr int TPF = NT / G;
   const int tid = threadIdx.x;
+  PreTw pt;
+  pt.thi = reinterpret_cast<const float2 *>(thi);
+  pt.tlo = reinterpret_cast<const float2 *>(tlo);
+  pt.h = a.tw_h;
+  pt.hmask = hmask;
+  pt.u0 = u0;
+  pt.Smask = Smask;
+  pt.Nsmask = Nsmask;
+  pt.inverse = a.inverse;
+  // FP32 passes after the first fold the conjugation and the inter-pass
+  // twiddles into their first stage (fast load path; radix 2^11 to 2^13, where
+  // the first stage keeps its inputs in registers without spilling)
+  pt.on = LOGR >= 11 && LOGR <= 13 && sizeof(T) == 4 && g_fast_in && !gx && a.nsum <= 1 &&
+          logNs > 0;
   if (g_fast_in && !gx) {
     const int g = tid % G, r0 = tid / G;
     const long long u = u0 + g;
@@ -418,7 +493,7 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
                        "l"(src + q * qs), "n"(sizeof(V))
                        : "memory");
         asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-        if (a.inverse || logNs > 0) {
+        if ((a.inverse || logNs > 0) && !pt.on) {
           // each thread rewrites only the elements it loaded: no barrier needed here
           TwRun tr;
           if constexpr (sizeof(T) == 4)
@@ -552,7 +627,7 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
   }
   __syncthreads();
   if constexpr (LOGR <= 9) rt_cta_fft<V, LOGR, G>(sm, twR);
-  else cta_fft<V, LOGR, G>(sm, twR);
+  else cta_fft<V, LOGR, G>(sm, twR, pt);
   V *__restrict__ out = reinterpret_cast<V *>(a.out);
   T *__restrict__ smp = reinterpret_cast<T *>(a.samples);
   const bool g_fast_out = logNs >= 0 && (1LL << logNs) >= G;

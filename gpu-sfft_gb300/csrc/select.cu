@@ -419,6 +419,10 @@ __device__ __forceinline__ unsigned ct_excl_scan(unsigned v, unsigned *ws, unsig
 
 template <typename K>
 __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(CoopArgs a) {
+  // Launched normally (it follows its predecessor completely); the trigger
+  // lets the next kernel's launch overlap this one, whose blocks are all
+  // resident already.
+  pdl_enter();
   cg::grid_group grid = cg::this_grid();
   // one private histogram per warp, two 16-bit counters per word, so warps
   // never contend on a bin (a warp counts at most chunk / 16 < 65536 keys)
