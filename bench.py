@@ -430,7 +430,9 @@ def run_ours(args, cfg):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16/f64-estimate (mixed)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": ("f32+bf16x3/f64-estimate (mixed)" if args.tc_bucket
+                  else "f32/f64-estimate (mixed)"),
         "data": "synthetic",
         "config": workload_config(cfg, {"global_batch": ws, "filter_design_ms_untimed":
                                         round(filter_ms, 1)}),
