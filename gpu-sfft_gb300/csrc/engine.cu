@@ -159,6 +159,13 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   if (s == GSFFT_OK) s = select_scratch_init(P->selB, p.loops_loc, p.B);
   if (s == GSFFT_OK) s = select_scratch_init(P->selW, p.RLFC_loops, p.W_RLFC);
   if (s == GSFFT_OK) s = select_scratch_init(P->selK, 1, P->cap);
+  if (s == GSFFT_OK &&
+      (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess)) {
+    set_last_error("plan init: %s", cudaGetErrorString(cudaGetLastError()));
+    s = GSFFT_ERR_CUDA;
+  }
   if (s == GSFFT_OK) {
     cudaError_t e = cudaMemset(P->vote, 0, sizeof(unsigned) * (size_t)p.n);
     if (e == cudaSuccess) e = cudaMemset(P->ctl, 0, sizeof(RunCtl));
@@ -187,6 +194,9 @@ void plan_destroy(Plan *P) {
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
+  if (P->ev_fork) cudaEventDestroy(P->ev_fork);
+  if (P->ev_join) cudaEventDestroy(P->ev_join);
+  if (P->side) cudaStreamDestroy(P->side);
   fft_plan_free(P->fftB);
   fft_plan_free(P->fftW);
   select_scratch_free(P->selB);
@@ -269,6 +279,10 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   if (ev) GS_CUDA(cudaEventRecord(ev[2 * (s)], st))
 #define END(s) \
   if (ev) GS_CUDA(cudaEventRecord(ev[2 * (s) + 1], st))
+#define BEGIN_ON(s, q) \
+  if (ev) GS_CUDA(cudaEventRecord(ev[2 * (s)], q))
+#define END_ON(s, q) \
+  if (ev) GS_CUDA(cudaEventRecord(ev[2 * (s) + 1], q))
   const bool quirk = (P->flags & GSFFT_FLAG_QUIRK_RESIDUE) != 0;
 
   // A5 (+ RLFC sub-sampling when streaming): bins of every loop
@@ -280,6 +294,33 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
     GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d, quirk,
                                 P->bins, st));
   END(ST_PERM_FILTER);
+
+  // A6: bucket FFT of every loop, cutoff of the location loops.  They need
+  // only the perm+filter, so they run on the plan's side stream beside A4's
+  // RLFC chain and join the main stream before the voting.
+  GS_CUDA(cudaEventRecord(P->ev_fork, st));
+  GS_CUDA(cudaStreamWaitEvent(P->side, P->ev_fork, 0));
+  BEGIN_ON(ST_BUCKET_FFT, P->side);
+  {
+    FftIo io;
+    io.samples = P->bsamp;
+    io.row_max = rmax_b;
+    io.err = &P->ctl->err;
+    const void *src = P->bins;
+    if (P->use_stream) {  // the row-group partials are added by the first pass
+      src = P->bpart;
+      io.sum_rows = P->groups;
+      io.sum_stride = (long long)p.loops * p.B;
+    }
+    GS_CHECK(fft_exec(P->fftB, src, P->bins, p.loops, -1, io, P->side));
+  }
+  END_ON(ST_BUCKET_FFT, P->side);
+  BEGIN_ON(ST_CUTOFF, P->side);
+  GS_CHECK(select_top(P->bsamp, kb, p.B, nullptr, p.B_thresh, p.loops_loc, p.B, P->J, p.B_thresh,
+                      nullptr, P->selB, P->side, rmax_b, P->floor_rel));
+  END_ON(ST_CUTOFF, P->side);
+
+  GS_CUDA(cudaEventRecord(P->ev_join, P->side));
 
   // A4: RLFC -- W-point FFT of the sub-sampled signal, |.|^2 epilogue, cutoff
   BEGIN(ST_RLFC_FFT);
@@ -310,28 +351,8 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
                                     P->bm_sig, P->ctl, st));
   END(ST_J2);
 
-  // A6: bucket FFT of every loop, cutoff of the location loops
-  BEGIN(ST_BUCKET_FFT);
-  {
-    FftIo io;
-    io.samples = P->bsamp;
-    io.row_max = rmax_b;
-    io.err = &P->ctl->err;
-    const void *src = P->bins;
-    if (P->use_stream) {  // the row-group partials are added by the first pass
-      src = P->bpart;
-      io.sum_rows = P->groups;
-      io.sum_stride = (long long)p.loops * p.B;
-    }
-    GS_CHECK(fft_exec(P->fftB, src, P->bins, p.loops, -1, io, st));
-  }
-  END(ST_BUCKET_FFT);
-  BEGIN(ST_CUTOFF);
-  GS_CHECK(select_top(P->bsamp, kb, p.B, nullptr, p.B_thresh, p.loops_loc, p.B, P->J, p.B_thresh,
-                      nullptr, P->selB, st, rmax_b, P->floor_rel));
-  END(ST_CUTOFF);
-
-  // A7: voting, one location loop after the other
+  // A7: voting, one location loop after the other (after the side stream)
+  GS_CUDA(cudaStreamWaitEvent(st, P->ev_join, 0));
   BEGIN(ST_VOTE);
   const size_t wW = (size_t)p.W_RLFC / 32;
   for (int l = 0; l < p.loops_loc; l++)
@@ -351,6 +372,8 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   END(ST_TOPK);
 #undef BEGIN
 #undef END
+#undef BEGIN_ON
+#undef END_ON
   P->launches_per_run = g_launch_counter - before;
   P->ran = true;
   return GSFFT_OK;

@@ -47,6 +47,9 @@ struct Plan {
   bool tc_bucket = false;  // bucket FFT with tensor-core passes
   double floor_rel = 1e-10;
   // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
+  // side stream of the bucket FFT and cutoff (they need only the perm+filter)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool timing = false;
   std::vector<cudaEvent_t> events;  // 2 * ST_COUNT per recorded run (begin, end)
   int timed_runs = 0;
