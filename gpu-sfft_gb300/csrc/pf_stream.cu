@@ -13,16 +13,20 @@
 // a bijection since a_l is odd), and tap j of that bucket sits in row
 //   r_j = (j*beta_l + s_l) mod nb,  beta_l = alpha_l^-1 mod nb,  s_l = -q_l*beta_l,
 // i.e. the column's hit rows are one per-loop set {j*beta_l mod nb} shifted by
-// s_l.  The host sorts that set once per run; a thread walks the rotated
-// copies of up to three loops of one column in ascending row order, so it
-// touches only its own ~3*w/B hits while the CTA (ceil(loops/3) threads per
-// column) streams every row of its 128 columns exactly once.  Sums run in
-// ascending row (= signal position) order: fixed, no atomics.
+// s_l.  The host sorts that set once per run; one thread per (column, loop)
+// walks its rotated copy in ascending row order, so it touches only its own
+// ~w/B hits while the CTA streams every row of its 64 (or 32) columns exactly
+// once.  Sums run in ascending row (= signal position) order: fixed, no
+// atomics.
 //
-// Tiles of rt rows x 128 columns arrive by cp.async.bulk.tensor.2d, issued
-// by a producer warp, into a three-stage shared-memory ring guarded by full /
-// empty mbarriers whose waits are bounded (a timeout sets an error flag
-// instead of hanging).
+// Tiles of rt rows x 64 columns arrive by cp.async.bulk.tensor.2d, issued by a
+// producer warp, into a shared-memory ring (three stages at two CTAs per SM;
+// four at one CTA per SM in the staged-tap form) guarded by full / empty
+// mbarriers whose waits are bounded (a timeout sets an error flag instead of
+// hanging).  Taps: in the staged form (FP32, up to 9 loops) each consumer
+// thread copies its bucket's taps into its own shared-memory slot with one
+// bulk copy per work item; otherwise each hit's tap is loaded from a
+// bucket-major table in L2, one hit ahead.
 //
 // RLFC loop r samples positions off_r + m*(n/W) (restLocFreqCoeffKernel,
 // innerLoop.cu:693-703); (n/W) divides B, so those are whole columns and the
@@ -150,9 +154,9 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 // Persistent, warp-specialised.  A work item is (block of CW columns, row
 // group); CTA b takes items b, b + grid, ...  Warp roles:
 //  * threads [0, CW*loops): consumers.  Thread (l, col) walks loop l of
-//    column col, so each warp covers 32 columns of one loop; the tap of its
-//    next hit is loaded one hit ahead (from the bucket-major tap table) so
-//    the L2 reads overlap the stream.
+//    column col, so each warp covers 32 columns of one loop; its taps come
+//    from its shared-memory slot (staged form) or from the bucket-major tap
+//    table one hit ahead, so the L2 reads overlap the stream.
 //  * the next warp: producer.  One lane streams every tile of the CTA's
 //    items, in order, into an NSTAGE ring (full[s]: tile landed, tx-counted;
 //    empty[s]: every releasing warp is done with it).
