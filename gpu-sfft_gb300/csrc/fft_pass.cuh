@@ -13,7 +13,9 @@
 // sequence of radix-16 register stages (one radix-2/4/8 stage for the
 // remainder).  G >= 2 (FP64) / 4 (FP32) so every strided global access moves
 // whole 32-byte sectors.  Twiddles come from exact-angle tables (sincospi in
-// FP64), never from recurrences.  Inverse = conj(DFT(conj(x))).
+// FP64); FP64 looks every one up, FP32 builds some as products of a few
+// looked-up ones (at most about eight roundings, never a long recurrence).
+// Inverse = conj(DFT(conj(x))).
 //
 // This header holds the pass kernel; its instantiations are spread over
 // fft_pass_*.cu so that they compile in parallel.
