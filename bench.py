@@ -684,6 +684,10 @@ def main():
         cfg.update(q=args.q, k=1000, Bcst=1.40, loops_est=5, RLFC_cst=128)
     if args.impl == "reference":
         return run_reference(args, cfg)
+    if args.workload == "batched256":
+        # 16 batch streams plus each plan's side stream: give them 32 hardware
+        # queues (read when the CUDA context is made, which has not happened yet)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     if args.workload in ("noisy40", "batched256", "largek8"):
         return run_configs(args)
     return run_ours(args, cfg)

@@ -357,6 +357,15 @@ int select_impl(const void *keys, long long size, const int *size_dev, int num, 
 // on the bits decided so far.  Counting and writing use per-thread runs of
 // contiguous samples and one packed block scan per sub-tile, so ids come out
 // ascending.  Histograms are left zeroed for the next call.
+//
+// Two launch forms of the same kernel, differing only in their barrier:
+//   - cooperative (CLU = false): one grid over all rows, `grid.sync()`; used
+//     for long rows, which need every SM's bandwidth;
+//   - one thread-block cluster per row (CLU = true): `cpr` <= 16 CTAs whose
+//     co-residency the hardware guarantees, `barrier.cluster` between passes.
+//     An ordinary launch, so selections of several plans on several streams
+//     run side by side (cooperative launches of different streams do not
+//     overlap), and its barrier is far cheaper than a grid-wide one.
 // ---------------------------------------------------------------------------
 namespace cg = cooperative_groups;
 
@@ -367,6 +376,10 @@ constexpr int CHUNK_MIN = 2048; // smallest chunk per CTA
 constexpr int UN = 8;           // loads in flight per thread in the scan passes
 constexpr int COOP_SMEM = (CT / 32) * (HIST_BINS / 2) * 4;  // per-warp histograms
 constexpr long long MAX_CHUNK = 16LL * 65535;  // keeps a warp's 16-bit counters exact
+constexpr int CLUSTER_MAX = 16;  // CTAs per row in the cluster form (non-portable size)
+// Rows up to this many samples (and top-k rows with a device-side live size)
+// take the cluster form.
+constexpr long long CLUSTER_ROW_MAX = 1LL << 18;
 // CTAs per SM the register budget is set for: three for 32-bit keys (the
 // large scans need the memory parallelism; two measured slower), two for
 // 64-bit keys (no spills; the top-k rows are short).
@@ -417,13 +430,19 @@ __device__ __forceinline__ unsigned ct_excl_scan(unsigned v, unsigned *ws, unsig
   return base + x - v;
 }
 
-template <typename K>
+template <typename K, bool CLU>
 __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(CoopArgs a) {
-  // Launched normally (it follows its predecessor completely); the trigger
-  // lets the next kernel's launch overlap this one, whose blocks are all
-  // resident already.
+  // Launched without programmatic serialization (it follows its predecessor
+  // completely); the trigger lets the next kernel's launch overlap this one,
+  // whose blocks are all resident already.
   pdl_enter();
-  cg::grid_group grid = cg::this_grid();
+  // Every barrier below is reached by all threads of all CTAs that take part
+  // in it: the conditions around them are uniform over the grid (cooperative
+  // form) or over the row's cluster (cluster form).
+  auto sync_all = [&]() {
+    if constexpr (CLU) cg::this_cluster().sync();
+    else cg::this_grid().sync();
+  };
   // one private histogram per warp, two 16-bit counters per word, so warps
   // never contend on a bin (a warp counts at most chunk / 16 < 65536 keys)
   extern __shared__ unsigned wh[];  // [CT / 32][HIST_BINS / 2]
@@ -466,7 +485,8 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
   int cmp_shift = 0;  // low bits ignored by the final comparisons
   bool done = take_all;
   bool counted = false;  // the chunk counts for the final threshold are already stored
-  // every row settled: grid-uniform, so every CTA skips the same grid syncs
+  // every row settled (the cluster form: this row settled): uniform over the
+  // CTAs sharing the barrier, so every one of them skips the same barriers
   bool all_done = take_all;
   // (grid-uniform condition: every CTA reaches the same grid syncs)
   if (a.row_max && a.floor_rel > 0.0) {
@@ -500,19 +520,25 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
       a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = tz;
       atomicAdd(&a.zero_count[b], tz);
     }
-    grid.sync();
-    // Every row's zero count is visible here and no longer changes, so every
-    // CTA reaches the same verdicts.  One thread per row loads them (every
-    // thread of every CTA loading the same words made an L2 hot spot).
-    if (tid < a.batch)
-      s_settled[tid] = !take_all && row_floor(tid) != 0 && (long long)__ldcg(&a.zero_count[tid]) > rank;
+    sync_all();
+    // The zero counts of the rows behind the barrier are visible here and no
+    // longer change, so every CTA reaches the same verdicts.  One thread per
+    // row loads them (every thread of every CTA loading the same words made
+    // an L2 hot spot).  The cluster form reads its own row only: other rows'
+    // clusters may still be counting.
+    if (CLU ? tid == 0 : tid < a.batch) {
+      const int r = CLU ? b : tid;
+      s_settled[r] = !take_all && row_floor(r) != 0 && (long long)__ldcg(&a.zero_count[r]) > rank;
+    }
     __syncthreads();
     if (s_settled[b]) {  // ascending rank `rank` is a zero
       done = true;
       counted = true;
     }
     bool all = !take_all;
-    for (int r = 0; r < a.batch; r++) all = all && s_settled[r];
+    if (CLU) all = all && s_settled[b];
+    else
+      for (int r = 0; r < a.batch; r++) all = all && s_settled[r];
     all_done = all_done || all;
   }
   int shift = kb;
@@ -565,7 +591,7 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
       }
       __syncthreads();  // the per-warp histograms are rebuilt next pass
     }
-    grid.sync();
+    sync_all();
     if (!done) {
       // the digit holding ascending rank `rank` of this row
       const unsigned *gh = a.hist + ((size_t)p * MAXB + b) * HIST_BINS;
@@ -601,7 +627,7 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
         done = true;  // every key of the bin was floored to exactly 0
       }
       if (p == npass - 1) done = true;
-      if (a.batch == 1) all_done = done;  // one row: its state is the grid's
+      if (CLU || a.batch == 1) all_done = done;  // one row behind the barrier
     }
   }
   // counting pass: (#greater, #equal) of this chunk
@@ -632,12 +658,19 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
     a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 0] = tgt;
     a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = teq;
   }
-  grid.sync();
-  if (blockIdx.x == 0 && tid < MAXB) a.zero_count[tid] = 0;  // read by every CTA before the sync above
-  // every CTA has read the histograms: zero them for the next call
-  for (long long i = (long long)blockIdx.x * CT + tid; i < (long long)npass * MAXB * HIST_BINS;
-       i += (long long)gridDim.x * CT)
-    a.hist[i] = 0;
+  sync_all();
+  // the zero counts and histograms were read by every CTA before the barrier
+  // above: zero them for the next call (the cluster form: its own row's)
+  if constexpr (CLU) {
+    if (ci == 0 && tid == 0) a.zero_count[b] = 0;
+    for (int i = ci * CT + tid; i < npass * HIST_BINS; i += a.cpr * CT)
+      a.hist[((size_t)(i / HIST_BINS) * MAXB + b) * HIST_BINS + (i % HIST_BINS)] = 0;
+  } else {
+    if (blockIdx.x == 0 && tid < MAXB) a.zero_count[tid] = 0;
+    for (long long i = (long long)blockIdx.x * CT + tid; i < (long long)npass * MAXB * HIST_BINS;
+         i += (long long)gridDim.x * CT)
+      a.hist[i] = 0;
+  }
   // writing pass
   int *o = a.out + (size_t)b * a.out_stride;
   if (take_all) {
@@ -709,10 +742,10 @@ int coop_grid() {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (!coop) return -1;
-    if (cudaFuncSetAttribute(sel_coop_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(sel_coop_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              COOP_SMEM) != cudaSuccess)
       return -1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K>, CT, COOP_SMEM);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K, false>, CT, COOP_SMEM);
     if (per > coop_ctas_per_sm<K>()) per = coop_ctas_per_sm<K>();
     g = per > 0 ? per * sms : -1;
   }
@@ -747,8 +780,85 @@ int select_coop_impl(const void *keys, long long size, const int *size_dev, int 
   a.zero_count = reinterpret_cast<unsigned *>(s.coop_hist) + 6 * MAXB * HIST_BINS;
   a.max_tiles = s.max_tiles;
   void *args[] = {&a};
-  GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K>, dim3((unsigned)(cpr * batch)),
+  GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K, false>, dim3((unsigned)(cpr * batch)),
                                       dim3(CT), args, COOP_SMEM, st));
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+// Largest cluster (CTAs per row) the device schedules for the cluster form:
+// 16 where non-portable sizes are allowed, else 8; 0 if clusters are not
+// available.
+template <typename K>
+int cluster_max() {
+  static int g = -1;
+  if (g < 0) {
+    g = 0;
+    if (cudaFuncSetAttribute(sel_coop_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             COOP_SMEM) != cudaSuccess)
+      return g;
+    const bool np = cudaFuncSetAttribute(sel_coop_kernel<K, true>,
+                                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+    for (int c = np ? CLUSTER_MAX : 8; c >= 2 && !g; c /= 2) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(c);
+      cfg.blockDim = dim3(CT);
+      cfg.dynamicSmemBytes = COOP_SMEM;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = c;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nc = 0;
+      if (cudaOccupancyMaxActiveClusters(&nc, sel_coop_kernel<K, true>, &cfg) == cudaSuccess && nc > 0) g = c;
+    }
+    cudaGetLastError();  // a refused size leaves no error behind
+  }
+  return g;
+}
+
+template <typename K>
+int select_cluster_impl(const void *keys, long long size, const int *size_dev, int num, int batch,
+                        long long row_stride, int *out, long long out_stride, int *count_out,
+                        SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
+  const int cmax = cluster_max<K>();
+  if (cmax <= 0) return GSFFT_ERR_UNSUPPORTED;
+  long long cpr = (size + CHUNK_MIN - 1) / CHUNK_MIN;
+  if (cpr > cmax) cpr = cmax;
+  if (cpr > s.max_tiles) cpr = s.max_tiles;
+  if (cpr < 1 || (size + cpr - 1) / cpr + 32 > MAX_CHUNK) return GSFFT_ERR_UNSUPPORTED;
+  CoopArgs a;
+  a.keys = keys;
+  a.size = size;
+  a.size_dev = size_dev;
+  a.num = num;
+  a.batch = batch;
+  a.cpr = (int)cpr;
+  a.row_stride = row_stride;
+  a.out = out;
+  a.out_stride = out_stride;
+  a.count_out = count_out;
+  a.row_max = row_max;
+  a.floor_rel = floor_rel;
+  a.hist = reinterpret_cast<unsigned *>(s.coop_hist);
+  a.tiles = reinterpret_cast<unsigned *>(s.tiles);
+  a.zero_count = reinterpret_cast<unsigned *>(s.coop_hist) + 6 * MAXB * HIST_BINS;
+  a.max_tiles = s.max_tiles;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(cpr * batch));
+  cfg.blockDim = dim3(CT);
+  cfg.dynamicSmemBytes = COOP_SMEM;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)cpr;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  GS_CUDA(cudaLaunchKernelEx(&cfg, sel_coop_kernel<K, true>, a));
   GS_LAUNCHED();
   return GSFFT_OK;
 }
@@ -788,6 +898,15 @@ int select_top(const void *keys, int key_bytes, long long size, const int *size_
   if (size_dev && batch != 1) return GSFFT_ERR_PARAM;
   if (g_select_coop && batch <= MAXB && batch <= s.max_batch &&
       (size + SEL_TILE - 1) / SEL_TILE <= s.max_tiles) {
+    if (size <= CLUSTER_ROW_MAX || size_dev) {
+      int r = key_bytes == 8
+                  ? select_cluster_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride,
+                                                            out, out_stride, count_out, s, st, row_max,
+                                                            floor_rel)
+                  : select_cluster_impl<unsigned int>(keys, size, size_dev, num, batch, row_stride, out,
+                                                      out_stride, count_out, s, st, row_max, floor_rel);
+      if (r != GSFFT_ERR_UNSUPPORTED) return r;
+    }
     int r = key_bytes == 8
                 ? select_coop_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride, out,
                                                        out_stride, count_out, s, st, row_max, floor_rel)

@@ -38,7 +38,8 @@ def test_fft_vs_numpy(G, torch_cuda, n, batch, prec):
 
 
 @pytest.mark.parametrize("size,num,batch", [(300, 7, 1), (5000, 2000, 2), (131072, 32000, 2),
-                                            (70001, 3, 1), (1 << 20, 4000, 2)])
+                                            (70001, 3, 1), (1 << 18, 5000, 8), ((1 << 18) + 1, 900, 3),
+                                            (1 << 20, 4000, 2)])
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("ties", [False, True])
 def test_cutoff_exact(G, O, torch_cuda, size, num, batch, prec, ties):
