@@ -495,7 +495,7 @@ int gsfft_stage_estimate(int precision, const int *d_cand, int num, const void *
     s = GSFFT_ERR_CUDA;
   if (s == GSFFT_OK) s = launch_hinv((const double2 *)d_filter_freq, n, nb, hinv, st);
   if (s == GSFFT_OK)
-    s = launch_estimate(precision, d_cand, ctl, num, d_bins, loops, n, B, d, hinv,
+    s = launch_estimate(precision, d_cand, ctl, num, num, d_bins, loops, n, B, d, hinv,
                         reinterpret_cast<DevNode *>(d_out), mag2, st);
   if (s == GSFFT_OK) s = sync_check(st, "gsfft_stage_estimate");
   cudaFree(hinv);

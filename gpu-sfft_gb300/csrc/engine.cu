@@ -20,6 +20,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
+
 namespace gsfft {
 
 namespace {
@@ -259,8 +261,13 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   }
   if (!capturing) GS_CHECK(plan_epoch_advance(P, st));
   const int kb = P->precision == GSFFT_FP64 ? 8 : 4;
-  run_begin_kernel<<<128, 256, 0, st>>>(P->ctl, (unsigned long long *)P->rmax, p.RLFC_loops + p.loops,
-                                        P->d_epoch, P->bm_sig, (long long)(p.W_RLFC / 32) * p.loops_loc);
+  {
+    // about eight bitmap words per thread, at most 128 CTAs
+    const long long bm_words = (long long)(p.W_RLFC / 32) * p.loops_loc;
+    const int grid = (int)std::min<long long>(128, std::max<long long>(1, (bm_words + 2047) / 2048));
+    run_begin_kernel<<<grid, 256, 0, st>>>(P->ctl, (unsigned long long *)P->rmax, p.RLFC_loops + p.loops,
+                                           P->d_epoch, P->bm_sig, bm_words);
+  }
   GS_LAUNCHED();
   void *rmax_w = P->rmax;  // RLFC rows, then bucket rows (u64 in FP64, u32 in FP32)
   void *rmax_b = (char *)P->rmax + (size_t)kb * p.RLFC_loops;
@@ -307,10 +314,15 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
     io.row_max = rmax_b;
     io.err = &P->ctl->err;
     const void *src = P->bins;
-    if (P->use_stream) {  // the row-group partials are added by the first pass
-      src = P->bpart;
-      io.sum_rows = P->groups;
-      io.sum_stride = (long long)p.loops * p.B;
+    if (P->use_stream) {
+      // The row-group partials are added in group order: by a kernel over
+      // every bin when there are several (a pass over few long rows would
+      // read them on a handful of CTAs), else the single group is the input.
+      if (P->groups > 1)
+        GS_CHECK(launch_sum_partials(P->precision, P->bpart, P->groups, (long long)p.loops * p.B,
+                                     P->bins, P->side));
+      else
+        src = P->bpart;
     }
     GS_CHECK(fft_exec(P->fftB, src, P->bins, p.loops, -1, io, P->side));
   }
@@ -362,7 +374,10 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   END(ST_VOTE);
   // A8: estimation; A9: k largest
   BEGIN(ST_ESTIMATE);
-  GS_CHECK(launch_estimate(P->precision, P->cand, P->ctl, P->cap, P->bins, p.loops, p.n, p.B, d,
+  // the grid covers 8k candidates at one per thread (about 4.8k at the
+  // 2^27 / 16000 workload); more are taken by the grid-stride loop
+  GS_CHECK(launch_estimate(P->precision, P->cand, P->ctl, P->cap,
+                           (int)std::min<long long>(P->cap, 8LL * p.k), P->bins, p.loops, p.n, p.B, d,
                            P->hinv, P->nodes, P->mag2, st));
   END(ST_ESTIMATE);
   BEGIN(ST_TOPK);

@@ -145,14 +145,15 @@ __global__ void gather_nodes_kernel(const DevNode *__restrict__ nodes, const int
 
 }  // namespace
 
-int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, const void *bins,
-                    int loops, int n, int B, const Draws &d, const double2 *hinv, DevNode *nodes,
-                    double *mag2, cudaStream_t st) {
+int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, int expect,
+                    const void *bins, int loops, int n, int B, const Draws &d, const double2 *hinv,
+                    DevNode *nodes, double *mag2, cudaStream_t st) {
   int lognb = 0;
   while ((1 << lognb) < n / B) lognb++;
   const unsigned nmask = (unsigned)n - 1u;
   if (loops >= 2 && loops <= 16) {
-    const int grid = min((cap + ET - 1) / ET, 152 * 8);
+    // sized for `expect` candidates; the grid-stride loop takes up to `cap`
+    const int grid = max(1, min((min(expect, cap) + ET - 1) / ET, 152 * 8));
 #define EST_CASE(LL)                                                                              \
   case LL:                                                                                        \
     if (precision == GSFFT_FP64)                                                                  \

@@ -436,6 +436,7 @@ __global__ void bucket_major_kernel(const V *__restrict__ filt, int w, int B, in
 
 template <typename V>
 __global__ void sum_partials_kernel(const V *__restrict__ part, int groups, long long count, V *out) {
+  pdl_enter();
   const long long i = (long long)blockIdx.x * 256 + threadIdx.x;
   if (i >= count) return;
   V v = part[i];
@@ -554,11 +555,11 @@ int launch_sum_partials(int precision, const void *part, int groups, long long c
                         cudaStream_t st) {
   const unsigned grid = (unsigned)((count + 255) / 256);
   if (precision == GSFFT_FP64)
-    sum_partials_kernel<double2><<<grid, 256, 0, st>>>((const double2 *)part, groups, count,
-                                                       (double2 *)out);
+    GS_CUDA(launch_pdl(sum_partials_kernel<double2>, dim3(grid), dim3(256), 0, st,
+                       (const double2 *)part, groups, count, (double2 *)out));
   else
-    sum_partials_kernel<float2><<<grid, 256, 0, st>>>((const float2 *)part, groups, count,
-                                                      (float2 *)out);
+    GS_CUDA(launch_pdl(sum_partials_kernel<float2>, dim3(grid), dim3(256), 0, st,
+                       (const float2 *)part, groups, count, (float2 *)out));
   GS_LAUNCHED();
   return GSFFT_OK;
 }

@@ -80,9 +80,11 @@ int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
 int vote_block_ints(int B_thresh);
 
 // A8: estimates + |value|^2 keys for the candidates.
-int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, const void *bins,
-                    int loops, int n, int B, const Draws &d, const double2 *hinv,
-                    DevNode *nodes, double *mag2, cudaStream_t st);
+// cap: candidate capacity; the grid is sized for `expect` candidates (a
+// grid-stride loop covers up to cap)
+int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, int expect,
+                    const void *bins, int loops, int n, int B, const Draws &d,
+                    const double2 *hinv, DevNode *nodes, double *mag2, cudaStream_t st);
 
 // 64-point complex DFTs of nvec float2 vectors on the tensor cores (tcgen05,
 // three-part bf16 split, fp32 accumulation); err: set when a wait timed out
