@@ -511,6 +511,12 @@ int launch_CW(const CUtensorMap &tm, const void *filt, int logn, int logB, int w
 inline bool pf_stream_staged(int cw, int rt, int loops, int tiles) {
   return pf_smem_bytes(8, cw, rt, loops, tiles, NSTAGE_STG, true) <= PF_SMEM_LIMIT;
 }
+// The same form for 10 to 15 loops (up to 1024 threads): the slots take more
+// room, so the ring keeps NSTAGE tiles.
+inline bool pf_stream_staged_wide(int cw, int rt, int loops, int tiles) {
+  return cw == 64 && 64 * loops + 64 <= 1024 &&
+         pf_smem_bytes(8, cw, rt, loops, tiles, NSTAGE, true) <= PF_SMEM_LIMIT;
+}
 
 template <typename T>
 int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int logB, int w, int rt,
@@ -527,6 +533,8 @@ int dispatch(int loops, const CUtensorMap &tm, const void *filt, int logn, int l
         if (pf_stream_staged(cw, rt, loops, tiles)) GO(64, 640, NSTAGE_STG, true);
       GO(64, 640, NSTAGE, false);
     }
+    if constexpr (sizeof(T) == 4)
+      if (pf_stream_staged_wide(cw, rt, loops, tiles)) GO(64, 1024, NSTAGE, true);
     GO(64, 1024, NSTAGE, false);
   }
   if (small) GO(32, 640, NSTAGE, false);
@@ -582,9 +590,10 @@ int stream_pf_groups(int n, int B, int w, int loops, int precision) {
   if (cudaGetDevice(&dev) == cudaSuccess)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int cw = cols_per_item(loops);
-  // the staged FP32 form runs one CTA per SM (the dispatch's choice)
-  const bool stg = precision != GSFFT_FP64 && cw == 64 && 64 * loops + 64 <= 640 &&
-                   pf_stream_staged(cw, rt, loops, w / B);
+  // the staged FP32 forms run one CTA per SM (the dispatch's choice)
+  const bool stg = precision != GSFFT_FP64 && cw == 64 &&
+                   (64 * loops + 64 <= 640 ? pf_stream_staged(cw, rt, loops, w / B)
+                                           : pf_stream_staged_wide(cw, rt, loops, w / B));
   // enough work items (column block x row group) for ~6 per persistent CTA,
   // each item at least four tiles long
   const long long want = 6LL * (stg ? 1 : CTAS_PER_SM) * sms;

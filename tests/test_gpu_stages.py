@@ -165,7 +165,8 @@ def test_estimate(G, O, torch_cuda, prec):
 
 @pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("n,B,w,loops", [(1 << 16, 256, 3479, 9), (1 << 20, 8192, 123349, 7),
-                                         (1 << 18, 8192, 200001, 2)])
+                                         (1 << 18, 8192, 200001, 2), (1 << 20, 8192, 123349, 11),
+                                         (1 << 18, 2048, 20000, 15)])
 def test_perm_filter_stream(G, O, torch_cuda, prec, n, B, w, loops):
     """The ordered pass over x computes the same bucket sums (taps of a bucket
     added in increasing signal position instead of increasing tap index)."""
