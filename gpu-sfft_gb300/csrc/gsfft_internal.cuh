@@ -177,7 +177,7 @@ struct SelectScratch {
   void *hist = nullptr;        // batch * 2048 uint32
   void *state = nullptr;       // batch * SelState
   void *tiles = nullptr;       // batch * max_tiles * 4 uint32
-  void *coop_hist = nullptr;   // single-launch form: 6 passes x 8 rows x 2048 bins, then 8 row counters
+  void *coop_hist = nullptr;   // single-launch form: 6 passes x 8 rows x 2048 bins, zero between calls
   int max_batch = 0, max_tiles = 0;
 };
 extern bool g_select_coop;  // use the single-launch cooperative select

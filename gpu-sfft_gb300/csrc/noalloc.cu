@@ -32,7 +32,6 @@ namespace {
 //   hist       rows x 2048 bins x 4             (multi-launch radix passes)
 //   state      rows x per-row selection state   (1 KiB reserved)
 //   coop_hist  6 passes x 8 rows x 2048 x 4     (single-launch form; zero on entry)
-//              + 8 per-row counters, padded to 256 bytes
 //   tiles      rows x (max_size / 4096) x 4 x 4 (per-tile counts)
 constexpr size_t kTile = 4096;  // samples per selection tile
 constexpr size_t kMaxTiles = (GSFFT_NOALLOC_MAX_SIZE + kTile - 1) / kTile;
@@ -41,7 +40,7 @@ constexpr size_t kHistBytes = (size_t)GSFFT_NOALLOC_MAX_BATCH * 2048 * 4;
 constexpr size_t kStateOff = kHistOff + kHistBytes;
 constexpr size_t kStateBytes = 1024;
 constexpr size_t kCoopOff = kStateOff + kStateBytes;
-constexpr size_t kCoopBytes = (size_t)6 * 8 * 2048 * 4 + 256;
+constexpr size_t kCoopBytes = (size_t)6 * 8 * 2048 * 4;
 constexpr size_t kTilesOff = kCoopOff + kCoopBytes;
 constexpr size_t kTilesBytes = (size_t)GSFFT_NOALLOC_MAX_BATCH * kMaxTiles * 4 * 4;
 constexpr size_t kScratchBytes = kTilesOff + kTilesBytes;

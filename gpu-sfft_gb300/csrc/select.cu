@@ -354,9 +354,14 @@ int select_impl(const void *keys, long long size, const int *size_dev, int num, 
 // itself.  A pass ends the descent early when the threshold's bin is "pure":
 // it holds one sample, or it is the first pass's digit 0 while the rounding
 // floor maps every key of that digit to exact zero.  Keys are then compared
-// on the bits decided so far.  Counting and writing use per-thread runs of
-// contiguous samples and one packed block scan per sub-tile, so ids come out
-// ascending.  Histograms are left zeroed for the next call.
+// on the bits decided so far; in the second case the first pass has already
+// stored every chunk's (nonzero, zero) counts, which are the (#greater,
+// #equal) counts of threshold 0, so the counting pass is skipped too (a
+// noiseless spectrum: one histogram pass and the write pass).  Counting and
+// writing use per-thread runs of contiguous samples and one packed block scan
+// per sub-tile, so ids come out ascending.  Rows that start on 16-byte
+// boundaries (with a capacity of whole 16-byte words) are read with 16-byte
+// loads.  Histograms are left zeroed for the next call.
 //
 // Two launch forms of the same kernel, differing only in their barrier:
 //   - cooperative (CLU = false): one grid over all rows, `grid.sync()`; used
@@ -374,6 +379,7 @@ constexpr int CT = 512;         // threads per CTA
 constexpr int SPT = 8;          // contiguous samples per thread in the write pass
 constexpr int CHUNK_MIN = 2048; // smallest chunk per CTA
 constexpr int UN = 8;           // loads in flight per thread in the scan passes
+constexpr int UQ = 4;           // 16-byte loads in flight per thread (aligned rows)
 constexpr int COOP_SMEM = (CT / 32) * (HIST_BINS / 2) * 4;  // per-warp histograms
 constexpr long long MAX_CHUNK = 16LL * 65535;  // keeps a warp's 16-bit counters exact
 constexpr int CLUSTER_MAX = 16;  // CTAs per row in the cluster form (non-portable size)
@@ -398,7 +404,6 @@ struct CoopArgs {
   double floor_rel;
   unsigned *hist;        // [6][MAXB][HIST_BINS], zero on entry and on exit
   unsigned *tiles;       // [MAXB][max_tiles][2]: per-chunk (#greater, #equal)
-  unsigned *zero_count;  // [MAXB] zeros per row, zero on entry and on exit
   int max_tiles;
 };
 
@@ -430,7 +435,71 @@ __device__ __forceinline__ unsigned ct_excl_scan(unsigned v, unsigned *ws, unsig
   return base + x - v;
 }
 
-template <typename K, bool CLU>
+// Calls fn(i, key) for every sample i in [lo, hi) of the row, its key read
+// as 0 below the floor; UN scalar loads per thread in flight, or (VEC: the
+// row and its capacity are 16-byte aligned) UQ 16-byte loads.  lo is a
+// multiple of 32 samples unless the chunk is empty (lo = hi = the live size,
+// which may fall inside a 16-byte word: hence the i >= lo test).
+template <typename K> __host__ __device__ constexpr int keys_per_quad() { return 16 / (int)sizeof(K); }
+
+template <typename K>
+__device__ __forceinline__ void unpack_quad(const uint4 &v, K (&ks)[keys_per_quad<K>()]) {
+  if constexpr (sizeof(K) == 4) {
+    ks[0] = v.x;
+    ks[1] = v.y;
+    ks[2] = v.z;
+    ks[3] = v.w;
+  } else {
+    ks[0] = (unsigned long long)v.x | ((unsigned long long)v.y << 32);
+    ks[1] = (unsigned long long)v.z | ((unsigned long long)v.w << 32);
+  }
+}
+
+template <typename K, bool VEC, class F>
+__device__ __forceinline__ void for_chunk_keys(const void *row, long long lo, long long hi, K floor,
+                                               F &&fn) {
+  const int tid = threadIdx.x;
+  if constexpr (VEC) {
+    constexpr int EPQ = keys_per_quad<K>();
+    const uint4 *rq = reinterpret_cast<const uint4 *>(row);
+    const long long q_lo = lo / EPQ, q_hi = (hi + EPQ - 1) / EPQ;
+    for (long long qb = q_lo; qb < q_hi; qb += (long long)CT * UQ) {
+      uint4 v[UQ];
+#pragma unroll
+      for (int u = 0; u < UQ; u++) {
+        const long long q = qb + (long long)u * CT + tid;
+        v[u] = q < q_hi ? __ldg(rq + q) : make_uint4(0u, 0u, 0u, 0u);
+      }
+#pragma unroll
+      for (int u = 0; u < UQ; u++) {
+        const long long q = qb + (long long)u * CT + tid;
+        K ks[EPQ];
+        unpack_quad<K>(v[u], ks);
+#pragma unroll
+        for (int e = 0; e < EPQ; e++) {
+          const long long i = q * EPQ + e;
+          if (q < q_hi && i >= lo && i < hi) fn(i, ks[e] < floor ? (K)0 : ks[e]);
+        }
+      }
+    }
+  } else {
+    for (long long base = lo; base < hi; base += (long long)CT * UN) {
+      K kv[UN];
+#pragma unroll
+      for (int u = 0; u < UN; u++) {
+        const long long i = base + (long long)u * CT + tid;
+        kv[u] = i < hi ? load_key<K>(row, i, floor) : (K)0;
+      }
+#pragma unroll
+      for (int u = 0; u < UN; u++) {
+        const long long i = base + (long long)u * CT + tid;
+        if (i < hi) fn(i, kv[u]);
+      }
+    }
+  }
+}
+
+template <typename K, bool CLU, bool VEC>
 __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(CoopArgs a) {
   // Launched without programmatic serialization (it follows its predecessor
   // completely); the trigger lets the next kernel's launch overlap this one,
@@ -452,10 +521,11 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
   __shared__ long long s_rank;
   __shared__ unsigned s_bincount;
   const int tid = threadIdx.x, lane = tid & 31;
-  const int kb = (int)sizeof(K) * 8;
+  constexpr int kb = (int)sizeof(K) * 8;
   const int w64[6] = {11, 11, 11, 11, 10, 10};
   const int w32[3] = {11, 11, 10};
-  const int npass = kb == 64 ? 6 : 3;
+  constexpr int npass = kb == 64 ? 6 : 3;
+  constexpr int shift0 = kb - 11;  // shift of the first pass's digit
   const int b = blockIdx.x / a.cpr, ci = blockIdx.x % a.cpr;
   // row state (identical in every CTA of the row)
   long long sz = a.size;
@@ -474,73 +544,25 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
     const float m = __uint_as_float(reinterpret_cast<const unsigned *>(a.row_max)[r]);
     return (K)__float_as_uint((float)((double)m * a.floor_rel));
   };
+  // With a floor of at least 2^shift0, every key is either 0 or at least the
+  // floor, so digit 0 of the first pass holds exactly the row's zeros.
+  auto zero_digit = [&](int r) -> bool { return (unsigned long long)row_floor(r) >= (1ull << shift0); };
   const K floor = row_floor(b);
+  const bool zdig = zero_digit(b);
   const bool take_all = sz <= a.num;
   const long long chunk = ((sz + a.cpr - 1) / a.cpr + 31) & ~31LL;
   const long long lo = (long long)ci * chunk < sz ? (long long)ci * chunk : sz;
   const long long hi = lo + chunk < sz ? lo + chunk : sz;
   const void *row = reinterpret_cast<const char *>(a.keys) + (size_t)b * a.row_stride * sizeof(K);
+  const long long rank0 = sz - a.num - 1;  // the same for every row (rows share one size)
   unsigned long long prefix = 0;
-  long long rank = sz - a.num - 1;
+  long long rank = rank0;
   int cmp_shift = 0;  // low bits ignored by the final comparisons
   bool done = take_all;
   bool counted = false;  // the chunk counts for the final threshold are already stored
   // every row settled (the cluster form: this row settled): uniform over the
   // CTAs sharing the barrier, so every one of them skips the same barriers
   bool all_done = take_all;
-  // (grid-uniform condition: every CTA reaches the same grid syncs)
-  if (a.row_max && a.floor_rel > 0.0) {
-    const bool mine_row = !take_all && floor != 0;
-    // With a rounding floor most samples of a noiseless spectrum read as 0.
-    // Count this chunk's zeros first: when the threshold's rank falls among
-    // the row's zeros the threshold is 0 and the per-chunk (nonzero, zero)
-    // counts are exactly the (#greater, #equal) counts the write pass needs.
-    unsigned nz = 0, zc = 0;
-    for (long long base = lo; mine_row && base < hi; base += (long long)CT * UN) {
-      K kv[UN];
-#pragma unroll
-      for (int u = 0; u < UN; u++) {
-        const long long i = base + (long long)u * CT + tid;
-        kv[u] = i < hi ? load_key<K>(row, i, floor) : (K)1;
-      }
-#pragma unroll
-      for (int u = 0; u < UN; u++) {
-        const long long i = base + (long long)u * CT + tid;
-        if (i < hi) {
-          nz += kv[u] != 0;
-          zc += kv[u] == 0;
-        }
-      }
-    }
-    unsigned tnz, tz;
-    ct_excl_scan(nz, ws, &tnz);
-    ct_excl_scan(zc, ws, &tz);
-    if (tid == 0 && mine_row) {
-      a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 0] = tnz;
-      a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = tz;
-      atomicAdd(&a.zero_count[b], tz);
-    }
-    sync_all();
-    // The zero counts of the rows behind the barrier are visible here and no
-    // longer change, so every CTA reaches the same verdicts.  One thread per
-    // row loads them (every thread of every CTA loading the same words made
-    // an L2 hot spot).  The cluster form reads its own row only: other rows'
-    // clusters may still be counting.
-    if (CLU ? tid == 0 : tid < a.batch) {
-      const int r = CLU ? b : tid;
-      s_settled[r] = !take_all && row_floor(r) != 0 && (long long)__ldcg(&a.zero_count[r]) > rank;
-    }
-    __syncthreads();
-    if (s_settled[b]) {  // ascending rank `rank` is a zero
-      done = true;
-      counted = true;
-    }
-    bool all = !take_all;
-    if (CLU) all = all && s_settled[b];
-    else
-      for (int r = 0; r < a.batch; r++) all = all && s_settled[r];
-    all_done = all_done || all;
-  }
   int shift = kb;
   for (int p = 0; p < npass && !all_done; p++) {
     const int width = kb == 64 ? w64[p] : w32[p];
@@ -552,28 +574,18 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
       unsigned *mine = wh + (tid >> 5) * (HIST_BINS / 2);
       for (int i = lane; i < HIST_BINS / 2; i += 32) mine[i] = 0;
       __syncwarp();
-      // UN independent loads per thread in flight before the histogram
-      // updates.  Digit 0 (floored zeros dominate the first pass of a
-      // noiseless spectrum) is counted in a register; other digits go to the
-      // warp's private table, where only collisions inside the warp remain.
+      // Digit 0 (floored zeros dominate the first pass of a noiseless
+      // spectrum) is counted in a register; other digits go to the warp's
+      // private table, where only collisions inside the warp remain.
       unsigned zeros = 0;
-      for (long long base = lo; base < hi; base += (long long)CT * UN) {
-        unsigned long long kv[UN];
-#pragma unroll
-        for (int u = 0; u < UN; u++) {
-          const long long i = base + (long long)u * CT + tid;
-          kv[u] = i < hi ? (unsigned long long)load_key<K>(row, i, floor) : ~0ull;
+      for_chunk_keys<K, VEC>(row, lo, hi, floor, [&](long long, K key) {
+        const unsigned long long k = (unsigned long long)key;
+        if ((k & hi_mask) == prefix) {
+          const unsigned digit = (unsigned)(k >> shift) & dmask;
+          if (digit == 0) zeros++;
+          else atomicAdd(&mine[digit >> 1], 1u << ((digit & 1u) * 16));
         }
-#pragma unroll
-        for (int u = 0; u < UN; u++) {
-          const long long i = base + (long long)u * CT + tid;
-          if (i < hi && (kv[u] & hi_mask) == prefix) {
-            const unsigned digit = (unsigned)(kv[u] >> shift) & dmask;
-            if (digit == 0) zeros++;
-            else atomicAdd(&mine[digit >> 1], 1u << ((digit & 1u) * 16));
-          }
-        }
-      }
+      });
       zeros = __reduce_add_sync(0xffffffffu, zeros);
       if (lane == 0 && zeros) atomicAdd(&mine[0], zeros);  // bin 0 = low half of word 0
       __syncthreads();
@@ -588,6 +600,13 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
         }
         if (lo16) atomicAdd(&gh[2 * word], lo16);
         if (hi16) atomicAdd(&gh[2 * word + 1], hi16);
+        // Bin 0 of the first pass is this chunk's zero count: with the
+        // threshold at 0, (nonzero, zero) are the (#greater, #equal) counts
+        // the write pass needs.
+        if (p == 0 && word == 0 && zdig) {
+          a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 0] = (unsigned)(hi - lo) - lo16;
+          a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = lo16;
+        }
       }
       __syncthreads();  // the per-warp histograms are rebuilt next pass
     }
@@ -619,38 +638,41 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
       rank = s_rank;
       const unsigned cnt = s_bincount;
       __syncthreads();
-      const bool zero_bin = p == 0 && (prefix >> shift) == 0 && (unsigned long long)floor >= (1ull << shift);
       if (cnt == 1) {
         cmp_shift = shift;
         done = true;
-      } else if (zero_bin) {
-        done = true;  // every key of the bin was floored to exactly 0
+      } else if (p == 0 && (prefix >> shift) == 0 && zdig) {
+        done = true;  // the threshold is a floored zero; its counts are stored
+        counted = true;
       }
       if (p == npass - 1) done = true;
-      if (CLU || a.batch == 1) all_done = done;  // one row behind the barrier
+    }
+    if (CLU || a.batch == 1) {
+      all_done = done;  // one row behind the barrier
+    } else if (p == 0) {
+      // Several rows: all of them settle here when each one's threshold is a
+      // floored zero.  Every CTA reads the same final bin-0 counts, so every
+      // CTA reaches the same verdict (one thread per row loads them: every
+      // thread loading the same words made an L2 hot spot).
+      if (tid < a.batch)
+        s_settled[tid] = zero_digit(tid) &&
+                         (long long)__ldcg(&a.hist[(size_t)tid * HIST_BINS]) > rank0;
+      __syncthreads();
+      bool all = true;
+      for (int r = 0; r < a.batch; r++) all = all && s_settled[r];
+      all_done = all;
     }
   }
   // counting pass: (#greater, #equal) of this chunk
   const K thr = (K)prefix;
   const unsigned long long thr_c = (unsigned long long)thr >> cmp_shift;
   unsigned gt = 0, eq = 0;
-  if (!take_all && !counted) {
-    for (long long base = lo; base < hi; base += (long long)CT * UN) {
-      unsigned long long kv[UN];
-#pragma unroll
-      for (int u = 0; u < UN; u++) {
-        const long long i = base + (long long)u * CT + tid;
-        kv[u] = i < hi ? (unsigned long long)load_key<K>(row, i, floor) : 0ull;
-      }
-#pragma unroll
-      for (int u = 0; u < UN; u++) {
-        const long long i = base + (long long)u * CT + tid;
-        const unsigned long long kc = kv[u] >> cmp_shift;
-        gt += i < hi && kc > thr_c;
-        eq += i < hi && kc == thr_c;
-      }
-    }
-  }
+  if (!take_all && !counted)
+    for_chunk_keys<K, VEC>(row, lo, hi, floor, [&](long long, K key) {
+      const unsigned long long kc = (unsigned long long)key >> cmp_shift;
+      gt += kc > thr_c;
+      eq += kc == thr_c;
+    });
   unsigned tgt, teq;
   ct_excl_scan(gt, ws, &tgt);
   ct_excl_scan(eq, ws, &teq);
@@ -659,14 +681,12 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
     a.tiles[((size_t)b * a.max_tiles + ci) * 2 + 1] = teq;
   }
   sync_all();
-  // the zero counts and histograms were read by every CTA before the barrier
-  // above: zero them for the next call (the cluster form: its own row's)
+  // the histograms were read by every CTA before the barrier above: zero
+  // them for the next call (the cluster form: its own row's)
   if constexpr (CLU) {
-    if (ci == 0 && tid == 0) a.zero_count[b] = 0;
     for (int i = ci * CT + tid; i < npass * HIST_BINS; i += a.cpr * CT)
       a.hist[((size_t)(i / HIST_BINS) * MAXB + b) * HIST_BINS + (i % HIST_BINS)] = 0;
   } else {
-    if (blockIdx.x == 0 && tid < MAXB) a.zero_count[tid] = 0;
     for (long long i = (long long)blockIdx.x * CT + tid; i < (long long)npass * MAXB * HIST_BINS;
          i += (long long)gridDim.x * CT)
       a.hist[i] = 0;
@@ -694,15 +714,39 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
     const unsigned need_eq = (unsigned)(a.num - (int)s_tg);
     unsigned gt_run = s_bg, eq_run = s_be;
     for (long long base = lo; base < hi; base += (long long)CT * SPT) {
-      const long long i0 = base + (long long)tid * SPT;
+      const long long i0 = base + (long long)tid * SPT;  // a multiple of SPT
       unsigned gm = 0, em = 0;  // bit q: sample i0 + q is greater / equal
+      if constexpr (VEC) {
+        constexpr int EPQ = keys_per_quad<K>();
+        static_assert(SPT % EPQ == 0, "whole 16-byte loads per run");
+        const uint4 *rq = reinterpret_cast<const uint4 *>(row) + i0 / EPQ;
+        uint4 v[SPT / EPQ];
 #pragma unroll
-      for (int q = 0; q < SPT; q++) {
-        const long long i = i0 + q;
-        if (i < hi) {
-          const unsigned long long kc = (unsigned long long)load_key<K>(row, i, floor) >> cmp_shift;
-          gm |= (unsigned)(kc > thr_c) << q;
-          em |= (unsigned)(kc == thr_c) << q;
+        for (int c = 0; c < SPT / EPQ; c++)
+          v[c] = i0 + c * EPQ < hi ? __ldg(rq + c) : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+        for (int c = 0; c < SPT / EPQ; c++) {
+          K ks[EPQ];
+          unpack_quad<K>(v[c], ks);
+#pragma unroll
+          for (int e = 0; e < EPQ; e++) {
+            const int q = c * EPQ + e;
+            if (i0 + q < hi) {
+              const unsigned long long kc = (unsigned long long)(ks[e] < floor ? (K)0 : ks[e]) >> cmp_shift;
+              gm |= (unsigned)(kc > thr_c) << q;
+              em |= (unsigned)(kc == thr_c) << q;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < SPT; q++) {
+          const long long i = i0 + q;
+          if (i < hi) {
+            const unsigned long long kc = (unsigned long long)load_key<K>(row, i, floor) >> cmp_shift;
+            gm |= (unsigned)(kc > thr_c) << q;
+            em |= (unsigned)(kc == thr_c) << q;
+          }
         }
       }
       unsigned tot;
@@ -733,7 +777,7 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
   if (a.count_out && ci == 0 && tid == 0) a.count_out[b] = take_all ? (int)sz : a.num;
 }
 
-template <typename K>
+template <typename K, bool VEC>
 int coop_grid() {
   static int g = 0;
   if (!g) {
@@ -742,62 +786,28 @@ int coop_grid() {
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (!coop) return -1;
-    if (cudaFuncSetAttribute(sel_coop_kernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(sel_coop_kernel<K, false, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              COOP_SMEM) != cudaSuccess)
       return -1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K, false>, CT, COOP_SMEM);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K, false, VEC>, CT, COOP_SMEM);
     if (per > coop_ctas_per_sm<K>()) per = coop_ctas_per_sm<K>();
     g = per > 0 ? per * sms : -1;
   }
   return g;
 }
 
-template <typename K>
-int select_coop_impl(const void *keys, long long size, const int *size_dev, int num, int batch,
-                     long long row_stride, int *out, long long out_stride, int *count_out,
-                     SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
-  const int maxg = coop_grid<K>();
-  if (maxg <= 0) return GSFFT_ERR_UNSUPPORTED;
-  long long cpr = (size + CHUNK_MIN - 1) / CHUNK_MIN;
-  if (cpr > maxg / batch) cpr = maxg / batch;
-  if (cpr > s.max_tiles) cpr = s.max_tiles;
-  if (cpr < 1 || (size + cpr - 1) / cpr + 32 > MAX_CHUNK) return GSFFT_ERR_UNSUPPORTED;
-  CoopArgs a;
-  a.keys = keys;
-  a.size = size;
-  a.size_dev = size_dev;
-  a.num = num;
-  a.batch = batch;
-  a.cpr = (int)cpr;
-  a.row_stride = row_stride;
-  a.out = out;
-  a.out_stride = out_stride;
-  a.count_out = count_out;
-  a.row_max = row_max;
-  a.floor_rel = floor_rel;
-  a.hist = reinterpret_cast<unsigned *>(s.coop_hist);
-  a.tiles = reinterpret_cast<unsigned *>(s.tiles);
-  a.zero_count = reinterpret_cast<unsigned *>(s.coop_hist) + 6 * MAXB * HIST_BINS;
-  a.max_tiles = s.max_tiles;
-  void *args[] = {&a};
-  GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K, false>, dim3((unsigned)(cpr * batch)),
-                                      dim3(CT), args, COOP_SMEM, st));
-  GS_LAUNCHED();
-  return GSFFT_OK;
-}
-
 // Largest cluster (CTAs per row) the device schedules for the cluster form:
 // 16 where non-portable sizes are allowed, else 8; 0 if clusters are not
 // available.
-template <typename K>
+template <typename K, bool VEC>
 int cluster_max() {
   static int g = -1;
   if (g < 0) {
     g = 0;
-    if (cudaFuncSetAttribute(sel_coop_kernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(sel_coop_kernel<K, true, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              COOP_SMEM) != cudaSuccess)
       return g;
-    const bool np = cudaFuncSetAttribute(sel_coop_kernel<K, true>,
+    const bool np = cudaFuncSetAttribute(sel_coop_kernel<K, true, VEC>,
                                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
     for (int c = np ? CLUSTER_MAX : 8; c >= 2 && !g; c /= 2) {
       cudaLaunchConfig_t cfg = {};
@@ -812,21 +822,25 @@ int cluster_max() {
       cfg.attrs = at;
       cfg.numAttrs = 1;
       int nc = 0;
-      if (cudaOccupancyMaxActiveClusters(&nc, sel_coop_kernel<K, true>, &cfg) == cudaSuccess && nc > 0) g = c;
+      if (cudaOccupancyMaxActiveClusters(&nc, sel_coop_kernel<K, true, VEC>, &cfg) == cudaSuccess && nc > 0)
+        g = c;
     }
     cudaGetLastError();  // a refused size leaves no error behind
   }
   return g;
 }
 
-template <typename K>
-int select_cluster_impl(const void *keys, long long size, const int *size_dev, int num, int batch,
-                        long long row_stride, int *out, long long out_stride, int *count_out,
-                        SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
-  const int cmax = cluster_max<K>();
-  if (cmax <= 0) return GSFFT_ERR_UNSUPPORTED;
+// One launch of the single-launch select: the cluster form (CLU) or the
+// cooperative form, with 16-byte key loads when every row and the row
+// capacity are 16-byte aligned.
+template <typename K, bool CLU, bool VEC>
+int select_single_launch(const void *keys, long long size, const int *size_dev, int num, int batch,
+                         long long row_stride, int *out, long long out_stride, int *count_out,
+                         SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
+  const int cap = CLU ? cluster_max<K, VEC>() : coop_grid<K, VEC>() / batch;
+  if (cap <= 0) return GSFFT_ERR_UNSUPPORTED;
   long long cpr = (size + CHUNK_MIN - 1) / CHUNK_MIN;
-  if (cpr > cmax) cpr = cmax;
+  if (cpr > cap) cpr = cap;
   if (cpr > s.max_tiles) cpr = s.max_tiles;
   if (cpr < 1 || (size + cpr - 1) / cpr + 32 > MAX_CHUNK) return GSFFT_ERR_UNSUPPORTED;
   CoopArgs a;
@@ -844,23 +858,47 @@ int select_cluster_impl(const void *keys, long long size, const int *size_dev, i
   a.floor_rel = floor_rel;
   a.hist = reinterpret_cast<unsigned *>(s.coop_hist);
   a.tiles = reinterpret_cast<unsigned *>(s.tiles);
-  a.zero_count = reinterpret_cast<unsigned *>(s.coop_hist) + 6 * MAXB * HIST_BINS;
   a.max_tiles = s.max_tiles;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(cpr * batch));
-  cfg.blockDim = dim3(CT);
-  cfg.dynamicSmemBytes = COOP_SMEM;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = (unsigned)cpr;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  GS_CUDA(cudaLaunchKernelEx(&cfg, sel_coop_kernel<K, true>, a));
+  if constexpr (CLU) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(cpr * batch));
+    cfg.blockDim = dim3(CT);
+    cfg.dynamicSmemBytes = COOP_SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)cpr;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    GS_CUDA(cudaLaunchKernelEx(&cfg, sel_coop_kernel<K, true, VEC>, a));
+  } else {
+    void *args[] = {&a};
+    GS_CUDA(cudaLaunchCooperativeKernel((const void *)sel_coop_kernel<K, false, VEC>,
+                                        dim3((unsigned)(cpr * batch)), dim3(CT), args, COOP_SMEM, st));
+  }
   GS_LAUNCHED();
   return GSFFT_OK;
+}
+
+template <typename K>
+int select_single(bool clu, const void *keys, long long size, const int *size_dev, int num, int batch,
+                  long long row_stride, int *out, long long out_stride, int *count_out,
+                  SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
+  const bool vec = reinterpret_cast<uintptr_t>(keys) % 16 == 0 &&
+                   ((unsigned long long)row_stride * sizeof(K)) % 16 == 0 &&
+                   ((unsigned long long)size * sizeof(K)) % 16 == 0;
+#define SEL_GO(C, V)                                                                                 \
+  return select_single_launch<K, C, V>(keys, size, size_dev, num, batch, row_stride, out, out_stride, \
+                                       count_out, s, st, row_max, floor_rel)
+  if (clu) {
+    if (vec) SEL_GO(true, true);
+    SEL_GO(true, false);
+  }
+  if (vec) SEL_GO(false, true);
+  SEL_GO(false, false);
+#undef SEL_GO
 }
 
 }  // namespace
@@ -873,8 +911,8 @@ int select_scratch_init(SelectScratch &s, int max_batch, long long max_size) {
   GS_CUDA(cudaMalloc(&s.state, sizeof(SelState) * max_batch));
   GS_CUDA(cudaMalloc(&s.tiles, sizeof(unsigned) * 4 * (size_t)s.max_tiles * max_batch));
   GS_CUDA(cudaMemset(s.state, 0, sizeof(SelState) * max_batch));
-  GS_CUDA(cudaMalloc(&s.coop_hist, sizeof(unsigned) * (6 * MAXB * HIST_BINS + MAXB)));
-  GS_CUDA(cudaMemset(s.coop_hist, 0, sizeof(unsigned) * (6 * MAXB * HIST_BINS + MAXB)));
+  GS_CUDA(cudaMalloc(&s.coop_hist, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
+  GS_CUDA(cudaMemset(s.coop_hist, 0, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
   return GSFFT_OK;
 }
 
@@ -898,21 +936,16 @@ int select_top(const void *keys, int key_bytes, long long size, const int *size_
   if (size_dev && batch != 1) return GSFFT_ERR_PARAM;
   if (g_select_coop && batch <= MAXB && batch <= s.max_batch &&
       (size + SEL_TILE - 1) / SEL_TILE <= s.max_tiles) {
-    if (size <= CLUSTER_ROW_MAX || size_dev) {
-      int r = key_bytes == 8
-                  ? select_cluster_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride,
+    for (const bool clu : {true, false}) {
+      if (clu && !(size <= CLUSTER_ROW_MAX || size_dev)) continue;
+      const int r = key_bytes == 8
+                        ? select_single<unsigned long long>(clu, keys, size, size_dev, num, batch, row_stride,
                                                             out, out_stride, count_out, s, st, row_max,
                                                             floor_rel)
-                  : select_cluster_impl<unsigned int>(keys, size, size_dev, num, batch, row_stride, out,
-                                                      out_stride, count_out, s, st, row_max, floor_rel);
+                        : select_single<unsigned int>(clu, keys, size, size_dev, num, batch, row_stride,
+                                                      out, out_stride, count_out, s, st, row_max, floor_rel);
       if (r != GSFFT_ERR_UNSUPPORTED) return r;
     }
-    int r = key_bytes == 8
-                ? select_coop_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride, out,
-                                                       out_stride, count_out, s, st, row_max, floor_rel)
-                : select_coop_impl<unsigned int>(keys, size, size_dev, num, batch, row_stride, out,
-                                                 out_stride, count_out, s, st, row_max, floor_rel);
-    if (r != GSFFT_ERR_UNSUPPORTED) return r;
   }
   if (key_bytes == 8)
     return select_impl<unsigned long long>(keys, size, size_dev, num, batch, row_stride, out,
