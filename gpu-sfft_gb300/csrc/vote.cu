@@ -25,7 +25,10 @@
 //    bijection), so the update is a plain read-modify-write without races.
 //  * Candidates (count reaching loops_thresh) are appended in canonical order
 //    (location loop, bucket index, window position) by a count pass and a
-//    write pass with per-block prefix sums.
+//    write pass with per-block prefix sums.  The count pass records each
+//    bucket's first STASH candidates in window order, so the write pass
+//    copies them instead of walking the window and the vote table again
+//    (buckets with more candidates are walked again).
 #include "stages.cuh"
 
 namespace gsfft {
@@ -227,10 +230,11 @@ __device__ __forceinline__ unsigned warp_excl_scan(unsigned v, unsigned *total) 
 }
 
 constexpr int WPB = VT / 32;  // buckets (warps) per block
+constexpr int STASH = 32;     // candidates recorded per heavy bucket by the count pass
 
 __global__ void __launch_bounds__(VT)
 vote_count_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, unsigned *vote, int *cnt,
-                  int *blk, int *blk_pre, RunCtl *ctl) {
+                  int *blk, int *blk_pre, int *stash, RunCtl *ctl) {
   pdl_enter();
   const unsigned epoch = *epoch_p;
   __shared__ unsigned ws[VT / 32];
@@ -240,32 +244,58 @@ vote_count_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, unsigned
   unsigned c = 0;
   if (t < w.Bt) {
     const unsigned nmask = (unsigned)w.n - 1u;
+    int *const slot = stash + (size_t)t * STASH;
+    unsigned recorded = 0;  // this bucket's candidates so far (warp-uniform)
     for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
       // up to four visited positions at a time: their table reads are
       // independent, so they overlap instead of paying one DRAM latency each
+      unsigned app = 0;  // bits of this lane's mask whose count reached the threshold
       while (mask) {
         unsigned loc[4], e[4];
         int nq = 0;
+        const unsigned before = mask;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           if (mask) {
-            const int b = __ffs(mask) - 1;
+            const int bq = __ffs(mask) - 1;
             mask &= mask - 1;
-            loc[q] = ((unsigned)pos(b) * w.a) & nmask;
+            loc[q] = ((unsigned)pos(bq) * w.a) & nmask;
             nq = q + 1;
           }
         }
 #pragma unroll
         for (int q = 0; q < 4; q++)
           if (q < nq) e[q] = vote[loc[q]];
+        unsigned hitq = 0;  // bit q: position q of this round reached the threshold
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           if (q < nq) {
             const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
             vote[loc[q]] = (epoch << 8) | cv;
-            c += (cv == thresh);
+            hitq |= (unsigned)(cv == thresh) << q;
           }
         }
+        // the round's positions are the lowest set bits of `before`, in order
+        unsigned taken = before & ~mask;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const unsigned low = taken & (0u - taken);
+          taken ^= low;
+          if ((hitq >> q) & 1u) app |= low;
+        }
+      }
+      c += (unsigned)__popc(app);
+      // window order: chunks, then lanes, then bits (as the write pass walks)
+      if (__any_sync(0xffffffffu, app != 0u)) {
+        unsigned ctot;
+        unsigned o = recorded + warp_excl_scan((unsigned)__popc(app), &ctot);
+        while (app) {
+          const int b = __ffs(app) - 1;
+          app &= app - 1;
+          if (o < (unsigned)STASH) slot[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
+          o++;
+        }
+        recorded += ctot;
       }
     });
   }
@@ -343,8 +373,8 @@ vote_mark_kernel(WalkArgs w, const unsigned *epoch_p, unsigned *vote) {
 
 __global__ void __launch_bounds__(VT)
 vote_write_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, const unsigned *__restrict__ vote,
-                  const int *__restrict__ cnt, const int *__restrict__ blk_pre, int nblk, int *cand,
-                  int cap, RunCtl *ctl) {
+                  const int *__restrict__ cnt, const int *__restrict__ blk_pre, int nblk,
+                  const int *__restrict__ stash, int *cand, int cap, RunCtl *ctl) {
   pdl_enter();
   __shared__ unsigned ws[VT / 32];
   __shared__ int is_last;
@@ -356,7 +386,14 @@ vote_write_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, const un
   const unsigned wpre = blk_excl_scan(c, ws, &tot);  // lane 0 of each warp carries its count
   long long next = (long long)base_prev + blk_pre[blockIdx.x] + __shfl_sync(0xffffffffu, wpre, 0);
   const unsigned cw = __shfl_sync(0xffffffffu, c, 0);
-  if (cw) {
+  if (cw && cw <= (unsigned)STASH) {
+    // recorded by the count pass in window order
+    const int *slot = stash + (size_t)t * STASH;
+    for (unsigned j = lane; j < cw; j += 32) {
+      const long long o = next + j;
+      if (o < cap) cand[o] = slot[j];
+    }
+  } else if (cw) {
     const unsigned nmask = (unsigned)w.n - 1u;
     const unsigned want = (*epoch_p << 8) | thresh;
     for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
@@ -465,17 +502,22 @@ int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
     GS_LAUNCHED();
     return GSFFT_OK;
   }
-  int *blk_pre = blk + grid + 1;  // blk holds 2 * (grid + 1) ints
+  // blk: 2 * (grid + 1) ints of block counts and prefixes, then STASH
+  // candidate slots per heavy bucket
+  int *blk_pre = blk + grid + 1;
+  int *stash = blk + 2 * (grid + 1);
   GS_CUDA(launch_pdl(vote_count_kernel, dim3(grid), dim3(VT), 0, st, w, epoch, (unsigned)loops_thresh,
-                     vote, cnt, blk, blk_pre, ctl));
+                     vote, cnt, blk, blk_pre, stash, ctl));
   GS_LAUNCHED();
   GS_CUDA(launch_pdl(vote_write_kernel, dim3(grid), dim3(VT), 0, st, w, epoch, (unsigned)loops_thresh,
-                     (const unsigned *)vote, (const int *)cnt, (const int *)blk_pre, grid, cand, cap,
-                     ctl));
+                     (const unsigned *)vote, (const int *)cnt, (const int *)blk_pre, grid,
+                     (const int *)stash, cand, cap, ctl));
   GS_LAUNCHED();
   return GSFFT_OK;
 }
 
-int vote_block_ints(int B_thresh) { return 2 * ((B_thresh + WPB - 1) / WPB + 1); }
+int vote_block_ints(int B_thresh) {
+  return 2 * ((B_thresh + WPB - 1) / WPB + 1) + B_thresh * STASH;
+}
 
 }  // namespace gsfft
