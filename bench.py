@@ -672,7 +672,7 @@ def main():
     ap.set_defaults(tc_bucket=False)
     ap.add_argument("--only-mixed", action="store_true",
                     help="time only the mixed path and print its stage times (profiling runs)")
-    ap.add_argument("--in-flight", dest="in_flight", type=int, default=4,
+    ap.add_argument("--in-flight", dest="in_flight", type=int, default=8,
                     help="signals in flight for the extra 'pipelined' figure (1: skip it)")
     args = ap.parse_args()
     if args.warmup < 3:

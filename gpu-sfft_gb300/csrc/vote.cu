@@ -133,13 +133,15 @@ __global__ void sigma_bits_kernel(const int *__restrict__ J2, const int *num_dev
 }
 
 // Same bitmaps straight from the RLFC blocks (duplicates set the same bit
-// twice), with the per-loop maximum reduced per warp before one atomic.
+// twice), with the per-loop maximum reduced over the block before one atomic
+// (one per warp queued thousands of atomics on the same word).
 __global__ void sigma_from_blocks_kernel(const int *__restrict__ J2b, int total, int W, Draws d,
                                          int loops_loc, unsigned *bms, int words_per_map,
                                          int *fmax) {
   pdl_enter();
+  __shared__ int wmax[MAX_LOOPS][VT / 32];
   const int m = blockIdx.x * VT + threadIdx.x;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const bool ok = m < total;
   const unsigned v = ok ? (unsigned)J2b[m] : 0u;
   for (int l = 0; l < loops_loc; l++) {
@@ -148,7 +150,13 @@ __global__ void sigma_from_blocks_kernel(const int *__restrict__ J2b, int total,
     int mx = ok ? (int)f : -1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if (lane == 0 && mx >= 0) atomicMax(&fmax[l], mx);
+    if (lane == 0) wmax[l][warp] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x < loops_loc) {
+    int mx = -1;
+    for (int wv = 0; wv < VT / 32; wv++) mx = max(mx, wmax[threadIdx.x][wv]);
+    if (mx >= 0) atomicMax(&fmax[threadIdx.x], mx);
   }
 }
 
