@@ -180,7 +180,7 @@ struct SelectScratch {
   void *coop_hist = nullptr;   // single-launch form: 6 passes x 8 rows x 2048 bins, zero between calls
   int max_batch = 0, max_tiles = 0;
 };
-extern bool g_select_coop;  // use the single-launch cooperative select
+extern bool g_select_coop;  // use the single-launch select (cluster or cooperative form)
 int select_scratch_init(SelectScratch &s, int max_batch, long long max_size);
 void select_scratch_free(SelectScratch &s);
 // row_max (optional, per row, bit pattern of the largest sample) with

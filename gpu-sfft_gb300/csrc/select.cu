@@ -928,7 +928,7 @@ int select_launches(int key_bytes) { return key_bytes == 8 ? 9 : 6; }
 
 size_t select_state_bytes() { return sizeof(SelState); }
 
-bool g_select_coop = true;  // single-launch select when the device supports it
+bool g_select_coop = true;  // single-launch select (cluster or cooperative) when the device supports it
 
 int select_top(const void *keys, int key_bytes, long long size, const int *size_dev, int num,
                int batch, long long row_stride, int *out, long long out_stride, int *count_out,
