@@ -600,6 +600,14 @@ def run_configs(args):
         try:
             batch.capture(ptrs, drs)
             ms_g = timed(lambda: batch.launch(stream=sh), args.steps)
+            if args.profile_range:
+                # one replay of the whole batch between cudaProfilerStart/Stop,
+                # for `ncu --profile-from-start off` (after the timed loop)
+                torch.cuda.synchronize()
+                torch.cuda.profiler.start()
+                batch.launch(stream=sh)
+                torch.cuda.synchronize()
+                torch.cuda.profiler.stop()
         except RuntimeError as e:
             print(f"graph form unavailable: {e}", file=sys.stderr)
         line = {"workload": "batched256", "metric": "sparse FFTs/sec, 256 mixed signals q=18..24",
@@ -672,6 +680,8 @@ def main():
     ap.set_defaults(tc_bucket=False)
     ap.add_argument("--only-mixed", action="store_true",
                     help="time only the mixed path and print its stage times (profiling runs)")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="batched256: replay the batch once more between cudaProfilerStart/Stop")
     ap.add_argument("--in-flight", dest="in_flight", type=int, default=8,
                     help="signals in flight for the extra 'pipelined' figure (1: skip it)")
     args = ap.parse_args()
