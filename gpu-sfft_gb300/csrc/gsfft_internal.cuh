@@ -190,9 +190,5 @@ int select_top(const void *keys, int key_bytes, long long size, const int *size_
                int num, int batch, long long row_stride, int *out, long long out_stride,
                int *count_out, SelectScratch &s, cudaStream_t st,
                const void *row_max = nullptr, double floor_rel = 0.0);
-int select_launches(int key_bytes);
-
-// ---------------------------------------------------------------- misc kernels
-int launch_grid(long long threads, int block);
 
 }  // namespace gsfft

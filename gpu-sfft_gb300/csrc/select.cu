@@ -924,8 +924,6 @@ void select_scratch_free(SelectScratch &s) {
   s.hist = s.state = s.tiles = s.coop_hist = nullptr;
 }
 
-int select_launches(int key_bytes) { return key_bytes == 8 ? 9 : 6; }
-
 size_t select_state_bytes() { return sizeof(SelState); }
 
 bool g_select_coop = true;  // single-launch select (cluster or cooperative) when the device supports it
