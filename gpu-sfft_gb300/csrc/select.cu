@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
     } else if (p == 0) {
       // Several rows: all of them settle here when each one's threshold is a
       // floored zero.  Every CTA reads the same final bin-0 counts, so every
-      // CTA reaches the same verdict (one thread per row loads them: every
+      // CTA reaches the same decision (one thread per row loads them: every
       // thread loading the same words made an L2 hot spot).
       if (tid < a.batch)
         s_settled[tid] = zero_digit(tid) &&

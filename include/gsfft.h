@@ -43,7 +43,7 @@ typedef enum {
   GSFFT_ERR_CAPACITY = 2,    /* candidate list larger than the plan's capacity */
   GSFFT_ERR_ALLOC = 3,       /* device or host allocation failed */
   GSFFT_ERR_CUDA = 4,        /* a CUDA runtime call failed (see gsfft_last_error) */
-  GSFFT_ERR_UNSUPPORTED = 5, /* size or mode outside what this build supports */
+  GSFFT_ERR_UNSUPPORTED = 5, /* size or mode outside what the library supports */
   GSFFT_ERR_STATE = 6        /* plan used before gsfft_plan_set_filter, or similar */
 } gsfft_status;
 
