@@ -59,3 +59,16 @@ def test_null_arguments_rejected(G):
     assert L.gsfft_plan_destroy(None) == G.ERR_PARAM
     p = G.Params()
     assert L.gsfft_plan_create(C.byref(p), 0, 0, 0, None) == G.ERR_PARAM
+
+
+def test_cutoff_arguments_rejected(G):
+    """The cutoff's argument checks run before any device work, as the
+    reference's asserts do (B_thresh < B: a cutoff keeps fewer than all)."""
+    L = G.lib()
+    fake = C.c_void_p(16)  # never dereferenced: every call below is rejected first
+    assert L.gsfft_cutoff(fake, 100, 100, 1, G.FP64, fake, None) == G.ERR_PARAM  # num == size
+    assert L.gsfft_cutoff(fake, 100, 101, 1, G.FP64, fake, None) == G.ERR_PARAM  # num > size
+    assert L.gsfft_cutoff(fake, 100, 0, 1, G.FP64, fake, None) == G.ERR_PARAM    # num < 1
+    assert L.gsfft_cutoff(fake, 0, 1, 1, G.FP64, fake, None) == G.ERR_PARAM      # empty row
+    assert L.gsfft_cutoff(fake, 100, 10, 0, G.FP64, fake, None) == G.ERR_PARAM   # no rows
+    assert L.gsfft_cutoff(None, 100, 10, 1, G.FP64, fake, None) == G.ERR_PARAM
