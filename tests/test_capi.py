@@ -72,3 +72,25 @@ def test_cutoff_arguments_rejected(G):
     assert L.gsfft_cutoff(fake, 0, 1, 1, G.FP64, fake, None) == G.ERR_PARAM      # empty row
     assert L.gsfft_cutoff(fake, 100, 10, 0, G.FP64, fake, None) == G.ERR_PARAM   # no rows
     assert L.gsfft_cutoff(None, 100, 10, 1, G.FP64, fake, None) == G.ERR_PARAM
+
+
+@pytest.mark.parametrize("field,value,status", [
+    ("n", 3000, "ERR_PARAM"),            # not a power of two
+    ("B", 3000, "ERR_PARAM"),
+    ("B_thresh", 0, "ERR_PARAM"),
+    ("B_thresh", 8192, "ERR_PARAM"),     # B_thresh >= B (the reference asserts B_thresh < B)
+    ("loops_thresh", 3, "ERR_PARAM"),    # loops_thresh > loops_loc
+    ("loops", 8, "ERR_PARAM"),           # loops != loops_loc + loops_est
+    ("RLFC_loops", 0, "ERR_PARAM"),
+    ("w", 0, "ERR_PARAM"),
+    ("W_RLFC", 1 << 20, "ERR_UNSUPPORTED"),  # W_RLFC = n
+    ("W_RLFC", 128, "ERR_PARAM"),            # B_thresh >= W_RLFC
+])
+def test_plan_create_rejects_params(G, field, value, status):
+    """Plan parameters are checked before any allocation (n = 2^20 base case)."""
+    p, st = G.derive_params(20, 1000, 1.40, 2, 2, 5, 128, 2)
+    assert st == G.OK
+    setattr(p, field, value)
+    h = C.c_void_p()
+    assert G.lib().gsfft_plan_create(C.byref(p), G.MIXED, 0, 0, C.byref(h)) == getattr(G, status)
+    assert not h.value
