@@ -94,3 +94,28 @@ def test_plan_create_rejects_params(G, field, value, status):
     h = C.c_void_p()
     assert G.lib().gsfft_plan_create(C.byref(p), G.MIXED, 0, 0, C.byref(h)) == getattr(G, status)
     assert not h.value
+
+
+def test_host_entry_points_reject_bad_arguments(G):
+    """Argument checks of the batch, ingest, conversion, filter-design,
+    evaluation and drop-in entry points, all before any device work."""
+    L = G.lib()
+    fake = C.c_void_p(16)  # never dereferenced: every call below is rejected first
+    h = C.c_void_p()
+    assert L.gsfft_batch_create(None, 1, 1, C.byref(h)) == G.ERR_PARAM
+    plans = (C.c_void_p * 1)(None)
+    assert L.gsfft_batch_create(plans, 0, 1, C.byref(h)) == G.ERR_PARAM
+    assert L.gsfft_batch_create(plans, 1, 1, C.byref(h)) == G.ERR_PARAM  # a null plan
+    assert L.gsfft_run_batched(None, None, None, None, None, None) == G.ERR_PARAM
+    assert L.gsfft_ingest(None, 10, G.FP64, fake, None) == G.ERR_PARAM
+    assert L.gsfft_ingest(fake, 0, G.FP64, fake, None) == G.ERR_PARAM
+    assert L.gsfft_ingest(fake, 10, 7, fake, None) == G.ERR_PARAM
+    assert L.gsfft_convert_signal(None, fake, 10, None) == G.ERR_PARAM
+    assert L.gsfft_convert_signal(fake, fake, 0, None) == G.ERR_PARAM
+    assert L.gsfft_design_filter(None, fake, fake, None) == G.ERR_PARAM
+    i1, i2, d1 = C.c_int(), C.c_int(), C.c_double()
+    assert L.gsfft_evaluate(None, fake, fake, 1, C.byref(i1), C.byref(i2), C.byref(d1),
+                            None) == G.ERR_PARAM
+    # the reference's outer_loop signature: NULL without an I_F pointer
+    assert L.outer_loop(fake, 1 << 20, fake, fake, 123349, 8192, 2000, 16384, 2, 2, 2, 7,
+                        None, 0.0) is None
