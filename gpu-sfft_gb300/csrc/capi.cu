@@ -549,7 +549,10 @@ Node *outer_loop(complex_t *d_x, int n, complex_t *d_filter_time, complex_t *d_f
     for (int it = 0; it < 5; it++) inv *= 2u - (unsigned)av * inv;
     ai[i] = (int)(inv & (unsigned)(n - 1));
   }
-  const unsigned flags = n < (1 << 27) ? GSFFT_FLAG_QUIRK_RESIDUE : 0u;
+  // the reference's own selection rule (raw |X|^2 threshold, innerLoop.cu:551-642) and,
+  // below n = 2^27, its residue tap index (innerLoop.cu:230-237, :745-754)
+  const unsigned flags =
+      GSFFT_FLAG_RAW_SELECTION | (n < (1 << 27) ? GSFFT_FLAG_QUIRK_RESIDUE : 0u);
   gsfft_plan plan = nullptr;
   Node *out = nullptr;
   int s = gsfft_plan_create(&p, GSFFT_FP64, flags, 524288, &plan);

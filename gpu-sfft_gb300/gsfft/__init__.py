@@ -109,6 +109,11 @@ def lib():
                                       C.POINTER(i), P], i),
         "gsfft_stage_estimate": ([i, P, i, P, i, i, i, P, P, P, P], i),
         "outer_loop": ([P, i, P, P, i, i, i, i, i, i, i, i, C.POINTER(i), C.c_float], P),
+        "restr_loc_freq_coeff": ([P, i, i, i, P, P], i),
+        "samples_indices": ([P, i, i, P, P], i),
+        "perm_filter_cutoff": ([P, i, P, i, i, i, i, i, P, P, P, P], i),
+        "reverse_hash": ([P, i, i, i, i, i, i, P, P, C.POINTER(i), P, P, i, i, i], i),
+        "estimate_values": ([P, C.POINTER(i), P, i, i, P, i, P, i], P),
         "timesmod": ([i, i, i], i),
     }
     for name, (args, res) in sig.items():

@@ -285,7 +285,8 @@ int gsfft_stage_estimate(int precision, const int *d_cand, int num, const void *
 
 /* outerLoop.h:35-38.  Draws the RLFC offsets with drand48() and the
  * permutations with random() in the reference's order, runs the FP64 engine
- * (residue quirk on for n < 2^27, like the reference's kernel switch at
+ * with the reference's selection rule (raw |X|^2 cutoffs, no floor) and,
+ * below n = 2^27, its residue tap index (the kernel switch at
  * innerLoop.cu:230) and returns a malloc'ed host array of *I_F Nodes
  * (caller frees).  d_filter_size is the tap count w.  Returns NULL on error
  * (message in gsfft_last_error). */

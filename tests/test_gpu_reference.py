@@ -1,0 +1,163 @@
+"""The engine against the reference implementation's own outputs (GPU).
+
+Two sources of reference outputs:
+  * the golden fixtures tests/golden/ref_*.npz (see tests/golden/make_ref_fixtures.py);
+  * live runs of the reference (pcdslab/gpu-sfft built from its own sources
+    into oracle/_ref/bin/ref_sfft by oracle/build_ref.py), at the n = 2^20,
+    k = 1000 configuration; skipped where that harness is not built.
+Every engine call goes through the C ABI: the stage drop-ins with the
+reference's signatures (innerLoop.h:32-50) and the native plan API.
+"""
+import ctypes as C
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import _refparity as RP
+
+pytestmark = pytest.mark.gpu
+
+CONFIG1 = (20, 1000, 1.4, 2, 2, 5, 128, 2)
+
+
+@pytest.mark.parametrize("case", RP.STAGE_CASES)
+def test_dropin_stage_matches_reference_fixture(G, torch_cuda, case):
+    meta, inp, ref = RP.load_stage(case)
+    got = RP.engine_stage(G, torch_cuda, RP.kind_of(case), meta, inp)
+    RP.check_stage(RP.kind_of(case), got, ref)
+
+
+def _run_plan(G, torch, f, precision):
+    p_g, st = G.derive_params(*f["cfg"])
+    assert st == 0
+    plan = G.Plan(p_g, precision, G.FLAG_RAW_SELECTION)
+    d_ft = torch.from_numpy(f["ft_dropped"]).cuda()
+    d_ff = torch.from_numpy(f["ff"]).cuda()
+    plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
+    x = torch.from_numpy(f["x"]).cuda()
+    if precision == G.MIXED:
+        x = x.to(torch.complex64)
+    offs, a, ai = f["draws"]
+    plan.run(x.data_ptr(), offs, a, ai)
+    res = plan.results()
+    plan.close()
+    assert res["status"] == 0
+    return RP.as_dict(res["nodes"])
+
+
+@pytest.mark.parametrize("name", RP.E2E_FIXTURES)
+def test_fp64_matches_reference_end_to_end(G, O, torch_cuda, name):
+    """FP64 path with the reference's signal, filter and glibc draws: the same
+    candidate set, values within 1e-9 relative, the same top-k location set."""
+    f = RP.load_e2e(O, name)
+    assert f["reps"][0] == f["reps"][1] == f["reps"][2]
+    got = _run_plan(G, torch_cuda, f, G.FP64)
+    RP.compare_e2e(got, f["reps"][0], f["p"].k, 1e-9)
+
+
+@pytest.mark.parametrize("name", RP.E2E_FIXTURES)
+def test_mixed_matches_reference_locations(G, O, torch_cuda, name):
+    """Mixed path (FP32 signal and buckets): the reference's top-k location
+    set, values within 1e-5 relative L2 on it."""
+    f = RP.load_e2e(O, name)
+    ref = f["reps"][0]
+    got = _run_plan(G, torch_cuda, f, G.MIXED)
+    k = f["p"].k
+    top = RP.topk_keys(ref, k)
+    assert RP.topk_keys(got, k) == top
+    r = np.array([ref[kk] for kk in sorted(top)])
+    g = np.array([got[kk] for kk in sorted(top)])
+    assert np.linalg.norm(g - r) <= 1e-5 * np.linalg.norm(r)
+
+
+@pytest.mark.parametrize("name", RP.E2E_FIXTURES[::2])
+def test_gpu_filter_design_matches_reference(G, O, torch_cuda, name):
+    f = RP.load_e2e(O, name)
+    p_g, st = G.derive_params(*f["cfg"])
+    torch = torch_cuda
+    d_ft = torch.zeros(p_g.w, dtype=torch.complex128, device="cuda")
+    d_ff = torch.zeros(p_g.n, dtype=torch.complex128, device="cuda")
+    G.design_filter(p_g, d_ft.data_ptr(), d_ff.data_ptr())
+    ft, ff = d_ft.cpu().numpy(), d_ff.cpu().numpy()
+    half = p_g.n // (2 * p_g.B)
+    win = np.r_[0:half + 1, p_g.n - half:p_g.n]
+    assert np.abs(ft - f["ft"]).max() <= 1e-10 * np.abs(f["ft"]).max()
+    assert np.abs(ff[win] - f["ff_win"]).max() <= 1e-10 * np.abs(f["ff_win"]).max()
+
+
+# ---- live reference runs --------------------------------------------------------
+
+def _ref():
+    from oracle import ref as R
+    if not R.available():
+        pytest.skip("reference harness not built (oracle/build_ref.py)")
+    return R
+
+
+_CASES = {}
+
+
+def _config1_cases():
+    if not _CASES:
+        from oracle import ref_cases
+        _CASES.update(ref_cases.build(CONFIG1, seed=3))
+    return _CASES
+
+
+@pytest.mark.parametrize("case", RP.STAGE_CASES)
+def test_dropin_stage_matches_live_reference_config1(G, O, torch_cuda, case):
+    """Stage drop-ins against the reference's own stage functions at the
+    n = 2^20, k = 1000 sizes (W = 16384, B = 8192), and the oracle as well."""
+    R = _ref()
+    meta, inp = _config1_cases()[case]
+    kind = RP.kind_of(case)
+    with tempfile.TemporaryDirectory() as tmp:
+        ref = RP.from_live(R.stage(kind, meta, inp, tmp))
+    RP.check_stage(kind, RP.engine_stage(G, torch_cuda, kind, meta, inp), ref)
+    RP.check_stage(kind, RP.oracle_stage(O, kind, meta, inp), ref)
+
+
+def _dropin(G, torch, D, seed):
+    prm = D["params"]
+    d_x = torch.from_numpy(D["x"]).cuda()
+    d_ft = torch.from_numpy(D["ft"]).cuda()
+    d_ff = torch.from_numpy(D["ff"]).cuda()
+    lc = C.CDLL(None)
+    lc.srand48(C.c_long(seed))
+    lc.srandom(C.c_uint(seed))
+    I_F = C.c_int(0)
+    ptr = G.lib().outer_loop(d_x.data_ptr(), prm["n"], d_ft.data_ptr(), d_ff.data_ptr(), prm["w"],
+                             prm["B"], prm["B_thresh"], prm["W_RLFC"], prm["RLFC_loops"],
+                             prm["loops_thresh"], prm["loops_loc"], prm["loops"], C.byref(I_F),
+                             C.c_float(0.0))
+    assert ptr, G.last_error()
+    nodes = np.ctypeslib.as_array((C.c_char * (24 * I_F.value)).from_address(ptr)).view(
+        G.NODE).copy()
+    lc.free(C.c_void_p(ptr))
+    return RP.as_dict(nodes)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_outer_loop_dropin_vs_live_reference_config1(G, torch_cuda, seed):
+    """The outer_loop drop-in against the reference's outer_loop on the
+    reference's own n = 2^20, k = 1000 experiment, same glibc seed.  At this
+    size the reference's perm+filter race (innerLoop.cu:745-754) makes its
+    own repeated runs differ in every value, so the comparison is on the
+    recovery: the true locations among the candidates, and those among the
+    k largest estimates, are the same."""
+    R = _ref()
+    with tempfile.TemporaryDirectory() as tmp:
+        R.run(CONFIG1, signal_seed=seed, outer_seed=100 + seed, reps=2, dump=tmp)
+        D = R.load_dump(tmp)
+    got = _dropin(G, torch_cuda, D, 100 + seed)
+    refs = [RP.as_dict(nd) for nd in D["nodes"]]
+    true = set(D["true_loc"].tolist())
+    k = D["params"]["k"]
+    found_ref = [true & set(r) for r in refs]
+    assert found_ref[0] == found_ref[1]
+    assert true & set(got) == found_ref[0]
+    top_ref = [true & RP.topk_keys(r, k) for r in refs]
+    if top_ref[0] == top_ref[1]:
+        assert true & RP.topk_keys(got, k) == top_ref[0]
