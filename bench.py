@@ -203,6 +203,33 @@ def run_reference(args, cfg):
     return 0
 
 
+def reference_cuda(cfg, candidates):
+    """Times the reference implementation (its own sources, built by
+    oracle/build_ref.py) on this GPU: one experiment at cfg whose outer_loop
+    the harness runs five times.  Returns None when the harness is not built.
+    The harness needs a candidate bound for n >= 2^20-class sizes (d_I has
+    MAXSIZE_HITS entries and no bound check, innerLoop.cu:813): 1.3 x this
+    engine's candidate count on the same configuration."""
+    from oracle import ref as R
+    if not R.available():
+        return None
+    if not candidates or 1.3 * candidates >= 524288 // 4:
+        return {"unavailable": "no safe candidate bound for the reference's unchecked d_I"}
+    try:
+        rep = R.run(cfg_args(cfg), reps=5, candidate_bound=int(1.3 * candidates), timeout=600)
+    except Exception as e:  # the reference exits on its own errors; report, do not fail
+        return {"unavailable": str(e)[-300:]}
+    ms = [t for _, t in rep["runs"]]
+    med = statistics.median(ms)
+    return {"value": 1e3 / med, "unit": UNIT, "ms_per_sfft_median": round(med, 3),
+            "ms_per_sfft": [round(t, 3) for t in ms],
+            "I_F": [c for c, _ in rep["runs"]], "missed_estimation_result": rep.get("missed"),
+            "sample": "pcdslab/gpu-sfft outer_loop (outerLoop.cu:65-190) built for sm_103a from its "
+                      "own sources, wall time of 5 calls on its own signal (k drand48 locations, "
+                      "values 1) and filter at this configuration, allocations and cuFFT plans "
+                      "inside each call as in the reference"}
+
+
 # ----------------------------------------------------------------------------
 # our arm
 # ----------------------------------------------------------------------------
@@ -236,9 +263,9 @@ def useful_bytes(p, es):
     return p.loops * p.w * es + p.RLFC_loops * p.W_RLFC * es + p.w * es + p.loops * p.B * es
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, from the ncu
-# captures summarised under profiles/ (keyed by kernel, form and workload):
-# profiles/pf_tma_kernel_stream_perm_filter.md.
+# DRAM bytes per launch of the dominant kernel: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one pf_tma_kernel launch on this workload (n = 2^27,
+# k = 16000, mixed), keyed by stage, perm+filter form and workload.
 TRAFFIC = {
     ("perm_filter", "stream", "q27k16000"): 1099172352 + 28483584,
 }
@@ -290,10 +317,12 @@ def run_ours(args, cfg):
         torch.cuda.synchronize()
 
     def timed(name, sampler=None):
+        """The timed region runs the steps bare (no per-stage events).  A
+        second pass over the same steps and draws, with CUDA events recorded
+        around every stage on the stream it runs on, gives the stage times."""
         pl, xx = plans[name], xin[name]
         for s in range(args.warmup):
             pl.run(xx.data_ptr(), *draws[s], stream=sh)
-        pl.enable_timing(True)
         barrier()
         if sampler:
             sampler.start()
@@ -305,6 +334,10 @@ def run_ours(args, cfg):
         barrier()
         clocks = sampler.stop() if sampler else None
         ms = e0.elapsed_time(e1)
+        pl.enable_timing(True)
+        pl.stage_times()  # restart the averages
+        for s in range(args.steps):
+            pl.run(xx.data_ptr(), *draws[args.warmup + s], stream=sh)
         stages, runs = pl.stage_times()
         pl.enable_timing(False)
         ms = max_over_ranks(ms, dist, dev)
@@ -393,18 +426,24 @@ def run_ours(args, cfg):
     form = plans["mixed"].describe()
     sb = stage_bytes(p, 8, form)
     dom = max(("perm_filter", "rlfc_fft", "bucket_fft"), key=lambda s: st32.get(s, 0.0))
-    achieved = sb[dom] / (st32[dom] * 1e-3) / 1e9
     form_name = "stream" if form["streaming"] else "gather"
     traffic = TRAFFIC.get((dom, form_name if dom == "perm_filter" else "", workload_key(cfg)))
+    launch_s = st32[dom] * 1e-3
+    # achieved = algorithmic bytes (what the stage must read and write whatever
+    # its access pattern) / the kernel's average launch time
+    algo = useful_bytes(p, 8) if dom == "perm_filter" else sb[dom]
+    achieved = algo / launch_s / 1e9
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
             "peak": peaks["hbm_gbs"], "peak_source": peak_src, "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
-            "algorithmic_bytes_per_launch": sb[dom], "launch_ms": round(st32[dom], 4),
-            "perm_filter_form": form_name}
-    if dom == "perm_filter":
-        ub = useful_bytes(p, 8)
-        roof["useful_bytes_per_launch"] = ub
-        roof["useful_frac"] = round(ub / (st32[dom] * 1e-3) / 1e9 / peaks["hbm_gbs"], 4)
+            "algorithmic_bytes_per_launch": algo, "launch_ms": round(st32[dom], 4),
+            "launch_ms_source": "CUDA events around the stage on its stream, second pass over "
+                                "the timed steps", "perm_filter_form": form_name}
+    if dom == "perm_filter" and form["streaming"]:
+        # the streaming form reads the whole signal once: its DRAM throughput
+        roof["streamed_bytes_per_launch"] = sb[dom]
+        roof["streamed_gbs"] = round(sb[dom] / launch_s / 1e9, 1)
+        roof["streamed_frac"] = round(sb[dom] / launch_s / 1e9 / peaks["hbm_gbs"], 4)
 
     # --- throughput with several signals in flight: P distinct signals, one
     # plan each, on P streams (gsfft_run_batched), fresh draws every step; the
@@ -461,6 +500,13 @@ def run_ours(args, cfg):
                "sample": f"{reps} full sparse FFTs of this workload, oracle/sfft_oracle.c with "
                          f"{cores} OpenMP threads"}
 
+    # --- the reference's own CUDA build on this GPU (rank 0, when built):
+    # its experiment at this configuration with its own signal generator,
+    # outer_loop timed five times by the harness (oracle/ref_harness.cu)
+    ref_cuda = None
+    if rank == 0 and not args.skip_reference_cuda:
+        ref_cuda = reference_cuda(cfg, acc.get("I_F"))
+
     launches = plans["mixed"].launches_per_run() * args.steps
     value = job_rate(ws, args.steps, ms32 * 1e-3)
     fp64 = job_rate(ws, args.steps, ms64 * 1e-3)
@@ -481,6 +527,7 @@ def run_ours(args, cfg):
         "accuracy": acc,
         "roofline": roof,
         "cpu_baseline": cpu,
+        "reference_cuda": ref_cuda,
         "e2e": {"value": job_rate(ws, args.steps, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -668,6 +715,8 @@ def main():
     ap.add_argument("--impl", default="gsfft", choices=["gsfft", "reference"])
     ap.add_argument("--q", type=int, default=None, help=argparse.SUPPRESS)  # smaller n for local checks
     ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-reference-cuda", action="store_true",
+                    help="do not time the reference's own CUDA build")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "small", "noisy40", "batched256", "largek8"],
                     help="small: n=2^25, k=4000 (same W_RLFC) for profiler captures")

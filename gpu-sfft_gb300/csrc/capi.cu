@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 namespace gsfft {
@@ -20,6 +21,39 @@ void set_last_error(const char *fmt, ...) {
   va_end(ap);
 }
 
+int current_ctx_key(CtxKey *out) {
+  typedef int (*CtxGetCurrent)(void **);
+  typedef int (*CtxGetId)(void *, unsigned long long *);
+  static CtxGetCurrent get_current = nullptr;
+  static CtxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetId>(f);
+  });
+  int dev = -1;
+  if (!get_current || !get_id || cudaGetDevice(&dev) != cudaSuccess) return GSFFT_ERR_CUDA;
+  void *ctx = nullptr;
+  if (get_current(&ctx) != 0) return GSFFT_ERR_CUDA;
+  if (!ctx) {
+    // no context yet on this thread: the runtime makes the device's primary
+    // context current on its first real call
+    if (cudaFree(nullptr) != cudaSuccess || get_current(&ctx) != 0 || !ctx) return GSFFT_ERR_CUDA;
+  }
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != 0) return GSFFT_ERR_CUDA;
+  out->dev = dev;
+  out->id = id;
+  return GSFFT_OK;
+}
+
 }  // namespace gsfft
 
 using namespace gsfft;
@@ -29,6 +63,29 @@ struct gsfft_plan_s {
 };
 
 static cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+namespace {
+// Largest sample of each row as a bit pattern (samples are non-negative, so
+// their bit patterns order like their values); out[] must start at zero.
+template <typename K>
+__global__ void row_max_kernel(const K *__restrict__ keys, long long size, int chunks,
+                               K *__restrict__ out) {
+  const int row = blockIdx.x / chunks, chunk = blockIdx.x % chunks;
+  const long long per = (size + chunks - 1) / chunks;
+  const long long lo = (long long)chunk * per;
+  const long long hi = lo + per < size ? lo + per : size;
+  K m = 0;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const K v = keys[(long long)row * size + i];
+    m = v > m ? v : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const K v = __shfl_down_sync(0xffffffffu, m, o);
+    m = v > m ? v : m;
+  }
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(out + row, m);
+}
+}  // namespace
 
 extern "C" {
 
@@ -330,6 +387,46 @@ int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precis
     set_last_error("gsfft_cutoff: %s", cudaGetErrorString(cudaGetLastError()));
     s = GSFFT_ERR_CUDA;
   }
+  select_scratch_free(ss);
+  return s;
+}
+
+
+int gsfft_cutoff_floor(const void *d_samples, int size, int num, int batch, int precision,
+                       double floor_rel, const void *d_row_max, int *d_out, void *stream) {
+  if (!d_samples || !d_out || size < 1 || num < 1 || num >= size || batch < 1 ||
+      !(floor_rel >= 0.0 && floor_rel < 1.0) ||
+      (precision != GSFFT_FP64 && precision != GSFFT_MIXED))
+    return GSFFT_ERR_PARAM;
+  const int kb = precision == GSFFT_FP64 ? 8 : 4;
+  cudaStream_t st = S(stream);
+  void *rmax = nullptr;
+  SelectScratch ss;
+  int s = select_scratch_init(ss, batch, size);
+  if (s == GSFFT_OK && !d_row_max && floor_rel > 0.0) {
+    if (cudaMalloc(&rmax, (size_t)kb * batch) != cudaSuccess) {
+      s = GSFFT_ERR_ALLOC;
+    } else if (cudaMemsetAsync(rmax, 0, (size_t)kb * batch, st) != cudaSuccess) {
+      s = GSFFT_ERR_CUDA;
+    } else {
+      const int chunks = (int)((size + 65535) / 65536);
+      if (kb == 8)
+        row_max_kernel<unsigned long long><<<batch * chunks, 256, 0, st>>>(
+            (const unsigned long long *)d_samples, size, chunks, (unsigned long long *)rmax);
+      else
+        row_max_kernel<unsigned><<<batch * chunks, 256, 0, st>>>((const unsigned *)d_samples, size,
+                                                                  chunks, (unsigned *)rmax);
+      if (cudaGetLastError() != cudaSuccess) s = GSFFT_ERR_CUDA;
+    }
+  }
+  if (s == GSFFT_OK)
+    s = select_top(d_samples, kb, size, nullptr, num, batch, size, d_out, num, nullptr, ss, st,
+                   d_row_max ? d_row_max : rmax, floor_rel);
+  if (s == GSFFT_OK && cudaStreamSynchronize(st) != cudaSuccess) {
+    set_last_error("gsfft_cutoff_floor: %s", cudaGetErrorString(cudaGetLastError()));
+    s = GSFFT_ERR_CUDA;
+  }
+  if (rmax) cudaFree(rmax);
   select_scratch_free(ss);
   return s;
 }

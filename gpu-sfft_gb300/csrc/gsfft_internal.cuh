@@ -5,9 +5,77 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <mutex>
+
 #include "gsfft.h"
 
 namespace gsfft {
+
+// ---------------------------------------------------------------- per-context set-up
+// The calling thread's current CUDA context: its device ordinal and the
+// driver's context id, which is unique for the life of the process (a context
+// made after cudaDeviceReset gets a new one).
+struct CtxKey {
+  int dev = -1;
+  unsigned long long id = 0;
+  bool operator==(const CtxKey &o) const { return dev == o.dev && id == o.id; }
+};
+int current_ctx_key(CtxKey *out);
+
+// One value per CUDA context, computed on first use in that context under a
+// lock.  Function attributes, occupancy figures and symbol addresses belong
+// to a context, so caching them process-wide would skip the set-up on a
+// second device, or after a device reset.
+template <typename T>
+class PerContext {
+ public:
+  template <typename F>
+  T get(F &&compute) {
+    CtxKey k;
+    if (current_ctx_key(&k) != 0) return compute();
+    std::lock_guard<std::mutex> lock(mu_);
+    for (int i = 0; i < n_; i++)
+      if (keys_[i] == k) return vals_[i];
+    const T v = compute();
+    if (n_ < kSlots) {
+      keys_[n_] = k;
+      vals_[n_] = v;
+      n_++;
+    }
+    return v;
+  }
+  // Calls set(want) unless this context already recorded a value >= want;
+  // records want when set returns 0.  For grow-only attributes such as the
+  // dynamic shared memory limit of a kernel.
+  template <typename F>
+  int ensure_at_least(T want, F &&set) {
+    CtxKey k;
+    if (current_ctx_key(&k) != 0) return set(want);
+    std::lock_guard<std::mutex> lock(mu_);
+    int i = 0;
+    for (; i < n_; i++)
+      if (keys_[i] == k) break;
+    if (i < n_ && !(vals_[i] < want)) return 0;
+    const int rc = set(want);
+    if (rc == 0) {
+      if (i < n_) {
+        vals_[i] = want;
+      } else if (n_ < kSlots) {
+        keys_[n_] = k;
+        vals_[n_] = want;
+        n_++;
+      }
+    }
+    return rc;
+  }
+
+ private:
+  static constexpr int kSlots = 64;
+  std::mutex mu_;
+  CtxKey keys_[kSlots];
+  T vals_[kSlots] = {};
+  int n_ = 0;
+};
 
 // ---------------------------------------------------------------- errors
 void set_last_error(const char *fmt, ...);
@@ -181,6 +249,14 @@ struct SelectScratch {
   int max_batch = 0, max_tiles = 0;
 };
 extern bool g_select_coop;  // use the single-launch select (cluster or cooperative form)
+// Byte sizes of the SelectScratch regions for max_batch rows of at most
+// max_size samples (what select_scratch_init allocates); state and coop_hist
+// must hold zeros when a selection starts.
+struct SelectScratchBytes {
+  size_t hist, state, tiles, coop_hist;
+  int max_tiles;
+};
+SelectScratchBytes select_scratch_bytes(int max_batch, long long max_size);
 int select_scratch_init(SelectScratch &s, int max_batch, long long max_size);
 void select_scratch_free(SelectScratch &s);
 // row_max (optional, per row, bit pattern of the largest sample) with

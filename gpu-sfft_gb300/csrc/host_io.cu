@@ -51,7 +51,7 @@ int staging_init(Staging &s) {
     return GSFFT_ERR_UNSUPPORTED;
   }
   for (int b = 0; b < 2; b++) {
-    GS_CUDA(cudaHostAlloc(&s.host[b], CHUNK * sizeof(complex_t), cudaHostAllocDefault));
+    GS_CUDA(cudaHostAlloc(&s.host[b], CHUNK * sizeof(complex_t), cudaHostAllocPortable));
     GS_CUDA(cudaMalloc(&s.dev[b], CHUNK * sizeof(double2)));
     GS_CUDA(cudaEventCreateWithFlags(&s.done[b], cudaEventDisableTiming));
   }

@@ -19,64 +19,63 @@
 // undefined results.
 #include "gsfft_internal.cuh"
 
-#include <mutex>
-
 namespace gsfft {
-
-size_t select_state_bytes();
 
 namespace {
 
-// Scratch layout (bytes), sized for GSFFT_NOALLOC_MAX_BATCH rows of at most
-// GSFFT_NOALLOC_MAX_SIZE samples:
-//   hist       rows x 2048 bins x 4             (multi-launch radix passes)
-//   state      rows x per-row selection state   (1 KiB reserved)
-//   coop_hist  6 passes x 8 rows x 2048 x 4     (single-launch form; zero on entry)
-//   tiles      rows x (max_size / 4096) x 4 x 4 (per-tile counts)
-constexpr size_t kTile = 4096;  // samples per selection tile
-constexpr size_t kMaxTiles = (GSFFT_NOALLOC_MAX_SIZE + kTile - 1) / kTile;
-constexpr size_t kHistOff = 0;
-constexpr size_t kHistBytes = (size_t)GSFFT_NOALLOC_MAX_BATCH * 2048 * 4;
-constexpr size_t kStateOff = kHistOff + kHistBytes;
-constexpr size_t kStateBytes = 1024;
-constexpr size_t kCoopOff = kStateOff + kStateBytes;
-constexpr size_t kCoopBytes = (size_t)6 * 8 * 2048 * 4;
-constexpr size_t kTilesOff = kCoopOff + kCoopBytes;
-constexpr size_t kTilesBytes = (size_t)GSFFT_NOALLOC_MAX_BATCH * kMaxTiles * 4 * 4;
-constexpr size_t kScratchBytes = kTilesOff + kTilesBytes;
-static_assert(kScratchBytes <= (size_t)1 << 20, "no-alloc scratch exceeds 1 MiB");
-static_assert(kStateOff % 256 == 0 && kCoopOff % 256 == 0 && kTilesOff % 256 == 0,
-              "scratch regions must stay 256-byte aligned");
+// The array is sized for GSFFT_NOALLOC_MAX_BATCH rows of at most
+// GSFFT_NOALLOC_MAX_SIZE samples.  Its regions are laid out at run time from
+// the selection's own size query (select_scratch_bytes), and every call
+// checks that they fit, so a change to the selection's scratch needs cannot
+// overrun the array: such a call returns GSFFT_ERR_UNSUPPORTED instead.
+constexpr size_t kScratchBytes = (size_t)1 << 20;
+constexpr size_t kAlign = 256;
 
 // One copy per device (a __device__ variable lives in every device's module).
 static __device__ __align__(256) unsigned char g_cutoff_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void *g_scratch_addr[kMaxDevices] = {};
+struct Layout {
+  size_t hist, state, coop, tiles, end;
+  SelectScratchBytes b;
+};
 
-// Device address of g_cutoff_scratch on the current device, looked up once per
-// device (the first call on a device makes the lookup, which may load this
-// library's device code onto that device).
+size_t round_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+Layout layout() {
+  Layout L;
+  L.b = select_scratch_bytes(GSFFT_NOALLOC_MAX_BATCH, GSFFT_NOALLOC_MAX_SIZE);
+  L.hist = 0;
+  L.state = round_up(L.hist + L.b.hist);
+  L.coop = round_up(L.state + L.b.state);
+  L.tiles = round_up(L.coop + L.b.coop_hist);
+  L.end = L.tiles + L.b.tiles;
+  return L;
+}
+
+// Device address of g_cutoff_scratch in the current context, looked up once
+// per context (the first call in a context makes the lookup, which may load
+// this library's device code there).  Keyed by context, not only by device,
+// so that a context made after cudaDeviceReset gets its own address.
 int scratch_address(void **out) {
-  int dev = 0;
-  GS_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_last_error("gsfft_cutoff_noalloc: device ordinal %d beyond %d", dev, kMaxDevices);
-    return GSFFT_ERR_UNSUPPORTED;
-  }
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_cutoff_scratch);
-    if (e != cudaSuccess || !p) {
-      set_last_error("gsfft_cutoff_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
-                     cudaGetErrorString(e));
-      return GSFFT_ERR_CUDA;
+  static PerContext<void *> cache;
+  const char *err = nullptr;
+  cudaError_t e = cudaSuccess;
+  void *p = cache.get([&]() -> void * {
+    void *a = nullptr;
+    e = cudaGetSymbolAddress(&a, g_cutoff_scratch);
+    if (e != cudaSuccess || !a) {
+      err = "cudaGetSymbolAddress failed";
+      return nullptr;
     }
-    g_scratch_addr[dev] = p;
+    return a;
+  });
+  if (!p) {
+    // a failed lookup is cached as nullptr for that context: report it
+    set_last_error("gsfft_cutoff_noalloc: %s: %s", err ? err : "no device address for the scratch",
+                   cudaGetErrorString(e));
+    return GSFFT_ERR_CUDA;
   }
-  *out = g_scratch_addr[dev];
+  *out = p;
   return GSFFT_OK;
 }
 
@@ -97,8 +96,10 @@ extern "C" int gsfft_cutoff_noalloc(const void *d_samples, int size, int num, in
                    batch, size, GSFFT_NOALLOC_MAX_BATCH, GSFFT_NOALLOC_MAX_SIZE);
     return GSFFT_ERR_CAPACITY;
   }
-  if (select_state_bytes() * GSFFT_NOALLOC_MAX_BATCH > kStateBytes) {
-    set_last_error("gsfft_cutoff_noalloc: selection state outgrew its scratch region");
+  const Layout L = layout();
+  if (L.end > kScratchBytes) {
+    set_last_error("gsfft_cutoff_noalloc: the selection needs %zu bytes of scratch, the fixed "
+                   "array holds %zu", L.end, kScratchBytes);
     return GSFFT_ERR_UNSUPPORTED;
   }
   void *base = nullptr;
@@ -106,15 +107,15 @@ extern "C" int gsfft_cutoff_noalloc(const void *d_samples, int size, int num, in
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   unsigned char *b = static_cast<unsigned char *>(base);
   SelectScratch ss;
-  ss.hist = b + kHistOff;
-  ss.state = b + kStateOff;
-  ss.coop_hist = b + kCoopOff;
-  ss.tiles = b + kTilesOff;
+  ss.hist = b + L.hist;
+  ss.state = b + L.state;
+  ss.coop_hist = b + L.coop;
+  ss.tiles = b + L.tiles;
   ss.max_batch = GSFFT_NOALLOC_MAX_BATCH;
-  ss.max_tiles = (int)kMaxTiles;
+  ss.max_tiles = L.b.max_tiles;
   // what the selection expects to find zeroed; the rest is written before it is read
-  GS_CUDA(cudaMemsetAsync(ss.state, 0, kStateBytes, st));
-  GS_CUDA(cudaMemsetAsync(ss.coop_hist, 0, kCoopBytes, st));
+  GS_CUDA(cudaMemsetAsync(ss.state, 0, L.b.state, st));
+  GS_CUDA(cudaMemsetAsync(ss.coop_hist, 0, L.b.coop_hist, st));
   // The SelectScratch does not own the array: it is never passed to
   // select_scratch_free.
   return select_top(d_samples, precision == GSFFT_FP64 ? 8 : 4, size, nullptr, num, batch, size,

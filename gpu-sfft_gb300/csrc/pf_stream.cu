@@ -484,12 +484,15 @@ int launch_CW(const CUtensorMap &tm, const void *filt, int logn, int logB, int w
   const int B = 1 << logB;
   const int smem = pf_smem_bytes((int)sizeof(V), CW, rt, loops, tiles, NS, STG);
   const int threads = CW * loops + (nrlfc > 0 ? 64 : 32);
-  static int attr = 0;
-  if (attr < smem) {
-    GS_CUDA(cudaFuncSetAttribute(pf_tma_kernel<T, CW, MAXTH, NS, STG>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr = smem;
-  }
+  static PerContext<int> attr;  // the kernel's dynamic shared memory limit, per context
+  GS_CHECK(attr.ensure_at_least(smem, [](int v) {
+    if (cudaFuncSetAttribute(pf_tma_kernel<T, CW, MAXTH, NS, STG>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, v) == cudaSuccess)
+      return (int)GSFFT_OK;
+    set_last_error("pf_tma_kernel: %d bytes of shared memory refused: %s", v,
+                   cudaGetErrorString(cudaGetLastError()));
+    return (int)GSFFT_ERR_CUDA;
+  }));
   int dev = 0, sms = 0, per_sm = 0;
   GS_CUDA(cudaGetDevice(&dev));
   GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -777,23 +777,26 @@ __global__ void __launch_bounds__(CT, coop_ctas_per_sm<K>()) sel_coop_kernel(Coo
   if (a.count_out && ci == 0 && tid == 0) a.count_out[b] = take_all ? (int)sz : a.num;
 }
 
+// CTAs of the cooperative form on the current device (-1: not available).
 template <typename K, bool VEC>
 int coop_grid() {
-  static int g = 0;
-  if (!g) {
+  static PerContext<int> cache;
+  return cache.get([] {
     int dev = 0, sms = 0, per = 0, coop = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (!coop) return -1;
     if (cudaFuncSetAttribute(sel_coop_kernel<K, false, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             COOP_SMEM) != cudaSuccess)
+                             COOP_SMEM) != cudaSuccess) {
+      cudaGetLastError();
       return -1;
+    }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sel_coop_kernel<K, false, VEC>, CT, COOP_SMEM);
+    cudaGetLastError();
     if (per > coop_ctas_per_sm<K>()) per = coop_ctas_per_sm<K>();
-    g = per > 0 ? per * sms : -1;
-  }
-  return g;
+    return per > 0 ? per * sms : -1;
+  });
 }
 
 // Largest cluster (CTAs per row) the device schedules for the cluster form:
@@ -801,12 +804,14 @@ int coop_grid() {
 // available.
 template <typename K, bool VEC>
 int cluster_max() {
-  static int g = -1;
-  if (g < 0) {
-    g = 0;
+  static PerContext<int> cache;
+  return cache.get([] {
+    int g = 0;
     if (cudaFuncSetAttribute(sel_coop_kernel<K, true, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             COOP_SMEM) != cudaSuccess)
+                             COOP_SMEM) != cudaSuccess) {
+      cudaGetLastError();
       return g;
+    }
     const bool np = cudaFuncSetAttribute(sel_coop_kernel<K, true, VEC>,
                                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
     for (int c = np ? CLUSTER_MAX : 8; c >= 2 && !g; c /= 2) {
@@ -826,8 +831,8 @@ int cluster_max() {
         g = c;
     }
     cudaGetLastError();  // a refused size leaves no error behind
-  }
-  return g;
+    return g;
+  });
 }
 
 // One launch of the single-launch select: the cluster form (CLU) or the
@@ -903,16 +908,28 @@ int select_single(bool clu, const void *keys, long long size, const int *size_de
 
 }  // namespace
 
+SelectScratchBytes select_scratch_bytes(int max_batch, long long max_size) {
+  SelectScratchBytes b;
+  b.max_tiles = (int)((max_size + SEL_TILE - 1) / SEL_TILE);
+  b.hist = sizeof(unsigned) * HIST_BINS * (size_t)max_batch;
+  b.state = sizeof(SelState) * (size_t)max_batch;
+  b.tiles = sizeof(unsigned) * 4 * (size_t)b.max_tiles * max_batch;
+  // single-launch form: one histogram per radix pass (at most 6) and row
+  b.coop_hist = sizeof(unsigned) * 6 * MAXB * HIST_BINS;
+  return b;
+}
+
 int select_scratch_init(SelectScratch &s, int max_batch, long long max_size) {
   select_scratch_free(s);
+  const SelectScratchBytes b = select_scratch_bytes(max_batch, max_size);
   s.max_batch = max_batch;
-  s.max_tiles = (int)((max_size + SEL_TILE - 1) / SEL_TILE);
-  GS_CUDA(cudaMalloc(&s.hist, sizeof(unsigned) * HIST_BINS * max_batch));
-  GS_CUDA(cudaMalloc(&s.state, sizeof(SelState) * max_batch));
-  GS_CUDA(cudaMalloc(&s.tiles, sizeof(unsigned) * 4 * (size_t)s.max_tiles * max_batch));
-  GS_CUDA(cudaMemset(s.state, 0, sizeof(SelState) * max_batch));
-  GS_CUDA(cudaMalloc(&s.coop_hist, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
-  GS_CUDA(cudaMemset(s.coop_hist, 0, sizeof(unsigned) * 6 * MAXB * HIST_BINS));
+  s.max_tiles = b.max_tiles;
+  GS_CUDA(cudaMalloc(&s.hist, b.hist));
+  GS_CUDA(cudaMalloc(&s.state, b.state));
+  GS_CUDA(cudaMalloc(&s.tiles, b.tiles));
+  GS_CUDA(cudaMemset(s.state, 0, b.state));
+  GS_CUDA(cudaMalloc(&s.coop_hist, b.coop_hist));
+  GS_CUDA(cudaMemset(s.coop_hist, 0, b.coop_hist));
   return GSFFT_OK;
 }
 

@@ -481,11 +481,15 @@ __global__ void __launch_bounds__(TP_THREADS, 1) tc4096_pass_kernel(TcPassArgs a
 }  // namespace
 
 int launch_tc_dft64(const void *x, void *y, int nvec, int *err, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    GS_CUDA(cudaFuncSetAttribute(tc_dft64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-    attr = true;
-  }
+  static PerContext<int> attr;  // the kernel's dynamic shared memory limit, per context
+  GS_CHECK(attr.ensure_at_least(TC_SMEM, [](int v) {
+    if (cudaFuncSetAttribute(tc_dft64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v) ==
+        cudaSuccess)
+      return (int)GSFFT_OK;
+    set_last_error("tc_dft64_kernel: %d bytes of shared memory refused: %s", v,
+                   cudaGetErrorString(cudaGetLastError()));
+    return (int)GSFFT_ERR_CUDA;
+  }));
   int dev = 0, sms = 0;
   GS_CUDA(cudaGetDevice(&dev));
   GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -505,11 +509,15 @@ int tc_build_F(void **F) {
 }
 
 int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    GS_CUDA(cudaFuncSetAttribute(tc4096_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC4K_SMEM));
-    attr = true;
-  }
+  static PerContext<int> attr;  // the kernel's dynamic shared memory limit, per context
+  GS_CHECK(attr.ensure_at_least(TC4K_SMEM, [](int v) {
+    if (cudaFuncSetAttribute(tc4096_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v) ==
+        cudaSuccess)
+      return (int)GSFFT_OK;
+    set_last_error("tc4096_pass_kernel: %d bytes of shared memory refused: %s", v,
+                   cudaGetErrorString(cudaGetLastError()));
+    return (int)GSFFT_ERR_CUDA;
+  }));
   if (a.logN < 12 || !a.tw_R) return GSFFT_ERR_UNSUPPORTED;
   int dev = 0, sms = 0;
   GS_CUDA(cudaGetDevice(&dev));

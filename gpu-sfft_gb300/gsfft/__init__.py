@@ -103,6 +103,7 @@ def lib():
         "gsfft_fft": ([P, P, ll, i, i, i, P], i),
         "gsfft_cutoff": ([P, i, i, i, i, P, P], i),
         "gsfft_cutoff_noalloc": ([P, i, i, i, i, P, P], i),
+        "gsfft_cutoff_floor": ([P, i, i, i, i, d, P, P, P], i),
         "gsfft_stage_perm_filter": ([i, P, i, P, i, i, i, P, i, P, P], i),
         "gsfft_stage_perm_filter_stream": ([i, P, i, P, i, i, i, P, P, P], i),
         "gsfft_stage_reverse_hash": ([P, i, P, i, i, i, i, i, i, i, u, P, P, i,
@@ -243,6 +244,14 @@ def ingest(h_x, precision, d_x, stream=0):
 
 def convert_signal(d_in, d_out, n, stream=0):
     check(lib().gsfft_convert_signal(d_in, d_out, n, stream or None), "gsfft_convert_signal")
+
+
+def cutoff_floor(d_samples, size, num, batch, precision, floor_rel, d_out, d_row_max=0,
+                 stream=0):
+    """gsfft_cutoff with the engine's selection floor (row maxima computed on
+    the device when d_row_max is 0)."""
+    check(lib().gsfft_cutoff_floor(d_samples, size, num, batch, precision, float(floor_rel),
+                                   d_row_max or None, d_out, stream or None), "gsfft_cutoff_floor")
 
 
 # limits of cutoff_noalloc (GSFFT_NOALLOC_MAX_SIZE / _BATCH in gsfft.h)

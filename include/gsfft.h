@@ -237,6 +237,15 @@ int gsfft_tc_dft64(const void *d_in, void *d_out, int nvec, void *stream);
 int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precision,
                  int *d_out, void *stream);
 
+/* The cutoff of the pipeline's RLFC and bucket stages: gsfft_cutoff with the
+ * selection floor, i.e. samples below floor_rel x the row's largest sample
+ * count as exact zeros, so that rounding-level samples tie and resolve by
+ * ascending index (innerLoop.cu:591-597's tie rule).  d_row_max: the largest
+ * sample of each row (double or float per precision), or NULL to have it
+ * computed here.  floor_rel = 0 is gsfft_cutoff.  Synchronises stream. */
+int gsfft_cutoff_floor(const void *d_samples, int size, int num, int batch, int precision,
+                       double floor_rel, const void *d_row_max, int *d_out, void *stream);
+
 /* No counterpart in the reference.  The same cutoff as gsfft_cutoff (same
  * arguments, same output) for callers that must not allocate device memory
  * while they run: a cudaMalloc/cudaFree can wait for the whole device to go
@@ -246,9 +255,9 @@ int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precis
  * of at most GSFFT_NOALLOC_MAX_SIZE samples; larger requests return
  * GSFFT_ERR_CAPACITY.  The work is queued on `stream` and the call returns
  * without waiting; d_out is ready once the stream reaches that point.
- * The first call on each device looks up the array's device address (and may
- * load this library's device code there), so make it before any stream
- * capture starts.  Every call on a device shares the array: calls that may
+ * The first call in each CUDA context (each device, and again after a
+ * cudaDeviceReset) looks up the array's device address (and may load this
+ * library's device code there), so make it before any stream capture starts.  Every call on a device shares the array: calls that may
  * overlap in time (other streams, unordered host threads) race and give
  * undefined results; calls ordered on one stream are safe. */
 #define GSFFT_NOALLOC_MAX_SIZE (1 << 24)
