@@ -700,12 +700,15 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
 template <typename T, int LOGR>
 int launch_pass(const PassArgs &a, long long total_sub, cudaStream_t st) {
   constexpr int G = g_of<T>(LOGR), NT = nt_of<T>(LOGR), SM = smem_of<T>(LOGR);
-  static bool attr_done = false;  // per instantiation; idempotent if raced
-  if (!attr_done) {
-    GS_CUDA(cudaFuncSetAttribute(fft_pass_kernel<T, LOGR>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-    attr_done = true;
-  }
+  static PerContext<int> attr;  // per instantiation and CUDA context
+  GS_CHECK(attr.ensure_at_least(SM, [](int v) {
+    if (cudaFuncSetAttribute(fft_pass_kernel<T, LOGR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             v) == cudaSuccess)
+      return (int)GSFFT_OK;
+    set_last_error("fft_pass_kernel: %d bytes of shared memory refused: %s", v,
+                   cudaGetErrorString(cudaGetLastError()));
+    return (int)GSFFT_ERR_CUDA;
+  }));
   long long grid = (total_sub + G - 1) / G;
   if (grid > 0x7fffffffLL) return GSFFT_ERR_UNSUPPORTED;
   GS_CUDA(launch_pdl(fft_pass_kernel<T, LOGR>, dim3((unsigned)grid), dim3(NT), SM, st, a));
