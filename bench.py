@@ -301,7 +301,8 @@ def run_ours(args, cfg):
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
     pf_flag = {"auto": 0, "gather": gsfft.FLAG_FORCE_GATHER, "stream": gsfft.FLAG_FORCE_STREAM}[args.pf]
-    tc_flag = gsfft.FLAG_TC_BUCKET_FFT if args.tc_bucket else 0
+    tc_flag = (gsfft.FLAG_TC_BUCKET_FFT if args.tc_bucket else 0) | \
+        (gsfft.FLAG_TC_RLFC_FFT if args.tc_rlfc else 0)
     plans = {"fp64": gsfft.Plan(p, gsfft.FP64, pf_flag),
              "mixed": gsfft.Plan(p, gsfft.MIXED, pf_flag | tc_flag)}
     for pl in plans.values():
@@ -514,8 +515,9 @@ def run_ours(args, cfg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f32+bf16x3/f64-estimate (mixed)" if args.tc_bucket
+        "dtype": ("f32+bf16x3/f64-estimate (mixed)" if (args.tc_bucket or args.tc_rlfc)
                   else "f32/f64-estimate (mixed)"),
+        "tensor_core_ffts": {"bucket": bool(args.tc_bucket), "rlfc": bool(args.tc_rlfc)},
         "data": "synthetic",
         "config": workload_config(cfg, {"global_batch": ws, "filter_design_ms_untimed":
                                         round(filter_ms, 1)}),
@@ -727,6 +729,11 @@ def main():
     ap.add_argument("--cc-bucket", dest="tc_bucket", action="store_false",
                     help="mixed bucket FFT on CUDA cores only")
     ap.set_defaults(tc_bucket=False)
+    ap.add_argument("--tc-rlfc", dest="tc_rlfc", action="store_true",
+                    help="mixed RLFC FFT with the tensor-core first pass")
+    ap.add_argument("--cc-rlfc", dest="tc_rlfc", action="store_false",
+                    help="mixed RLFC FFT on CUDA cores only")
+    ap.set_defaults(tc_rlfc=False)
     ap.add_argument("--only-mixed", action="store_true",
                     help="time only the mixed path and print its stage times (profiling runs)")
     ap.add_argument("--profile-range", action="store_true",

@@ -374,6 +374,38 @@ int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sig
   return s;
 }
 
+int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
+                 void *stream) {
+  if (!d_in || !d_out || batch < 1 || (sign != 1 && sign != -1)) return GSFFT_ERR_PARAM;
+  FftPlan fp;
+  int s = fft_plan_init_tc(fp, n_fft, batch);
+  if (s == GSFFT_OK) {
+    int *err = nullptr;
+    if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+      s = GSFFT_ERR_ALLOC;
+    } else {
+      FftIo io;
+      io.err = err;
+      if (cudaMemsetAsync(err, 0, sizeof(int), S(stream)) != cudaSuccess) s = GSFFT_ERR_CUDA;
+      if (s == GSFFT_OK) s = fft_exec(fp, d_in, d_out, batch, sign, io, S(stream));
+      int h = 0;
+      if (s == GSFFT_OK &&
+          (cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, S(stream)) != cudaSuccess ||
+           cudaStreamSynchronize(S(stream)) != cudaSuccess)) {
+        set_last_error("gsfft_fft_tc: %s", cudaGetErrorString(cudaGetLastError()));
+        s = GSFFT_ERR_CUDA;
+      }
+      if (s == GSFFT_OK && h) {
+        set_last_error("gsfft_fft_tc: a tensor-core completion wait timed out");
+        s = GSFFT_ERR_CUDA;
+      }
+      cudaFree(err);
+    }
+  }
+  fft_plan_free(fp);
+  return s;
+}
+
 int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precision, int *d_out,
                  void *stream) {
   if (!d_samples || !d_out || size < 1 || num < 1 || num >= size || batch < 1)

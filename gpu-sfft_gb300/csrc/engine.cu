@@ -157,7 +157,16 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
     P->tc_bucket = t == GSFFT_OK;
     if (!P->tc_bucket) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
   }
-  if (s == GSFFT_OK) s = fft_plan_init(P->fftW, p.W_RLFC, precision, p.RLFC_loops);
+  if (s == GSFFT_OK) {
+    // the RLFC transform reads the streaming pass's sub-samples; its first
+    // pass can then run on the tensor cores (the gather form fuses a strided
+    // gather into that pass instead)
+    int t = GSFFT_ERR_UNSUPPORTED;
+    if (precision == GSFFT_MIXED && (flags & GSFFT_FLAG_TC_RLFC_FFT) && P->use_stream)
+      t = fft_plan_init_tc(P->fftW, p.W_RLFC, p.RLFC_loops);
+    P->tc_rlfc = t == GSFFT_OK;
+    if (!P->tc_rlfc) s = fft_plan_init(P->fftW, p.W_RLFC, precision, p.RLFC_loops);
+  }
   if (s == GSFFT_OK) s = select_scratch_init(P->selB, p.loops_loc, p.B);
   if (s == GSFFT_OK) s = select_scratch_init(P->selW, p.RLFC_loops, p.W_RLFC);
   if (s == GSFFT_OK) s = select_scratch_init(P->selK, 1, P->cap);

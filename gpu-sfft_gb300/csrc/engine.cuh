@@ -45,6 +45,7 @@ struct Plan {
   int groups = 1;
   bool use_stream = false;
   bool tc_bucket = false;  // bucket FFT with tensor-core passes
+  bool tc_rlfc = false;    // RLFC FFT with a tensor-core first pass
   double floor_rel = 1e-10;
   // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
   // side stream of the bucket FFT and cutoff (they need only the perm+filter)

@@ -198,18 +198,21 @@ tc_dft64_kernel(const float2 *__restrict__ x, float2 *__restrict__ y, int nvec, 
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N) : "memory");
 }
 
-// The three bf16 parts of F (real form of DFT_64) in the K-major layout,
-// 3 x 32 KiB, built once per FFT plan.
+// The three bf16 parts of F' (the real form of DFT_64 with the real and
+// imaginary rows of each output interleaved: row 2o = Re, row 2o + 1 = Im of
+// output o) in the K-major layout, 3 x 32 KiB, built once per FFT plan.
+// With theta = 2 pi o i / 64 and W = e^{-i theta}:
+//   Re(W x) = cos(theta) xr + sin(theta) xi,  Im(W x) = cos(theta) xi - sin(theta) xr.
 __global__ void tc_build_F_kernel(unsigned char *F) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= TC_M * TC_K) return;
   const int m = e / TC_K, k = e % TC_K;
-  const int o = m & 63, i = k & 63;
+  const int o = m >> 1, i = k & 63;
   double s, c;
-  sincospi(-2.0 * (double)((o * i) & 63) / 64.0, &s, &c);
+  sincospi(2.0 * (double)((o * i) & 63) / 64.0, &s, &c);
   float f;
-  if (m < 64) f = (k < 64) ? (float)c : (float)(-s);
-  else f = (k < 64) ? (float)s : (float)c;
+  if ((m & 1) == 0) f = (k < 64) ? (float)c : (float)s;
+  else f = (k < 64) ? (float)(-s) : (float)c;
   __nv_bfloat16 p0, p1, p2;
   split3(f, p0, p1, p2);
   const int off = kmajor_off(m, k, TC_K);
@@ -218,21 +221,23 @@ __global__ void tc_build_F_kernel(unsigned char *F) {
   *reinterpret_cast<__nv_bfloat16 *>(F + 2 * A_BYTES + off) = p2;
 }
 
-constexpr int TP_THREADS = 256;  // two warpgroups: TMEM quadrant = warp % 4
-constexpr int DP = 68;           // row pitch (floats) of the fp32 result staged in shared memory
+// ---- radix-4096 pass ------------------------------------------------------
+constexpr int TP_THREADS = 256;  // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31
+constexpr int TP_N = 128;        // vectors per product: two sub-transforms x 64
+constexpr int X_BYTES = TP_N * TC_K * 2;  // one bf16 part of the X operand: 32 KiB
+constexpr int TW_BYTES = 4096 * 8;        // exp(-2 pi i m / 4096), m < 4096
+constexpr int TC4K_SMEM = 3 * A_BYTES + 3 * X_BYTES + TW_BYTES + 64;
+static_assert(TC4K_SMEM <= 227 * 1024, "radix-4096 pass exceeds the shared memory of a CTA");
 
-constexpr int ST_BYTES = 128 * DP * 4;  // fp32 staging of a 128 x 64 result
-constexpr int TC4K_SMEM = 3 * A_BYTES + 3 * B_BYTES + ST_BYTES + 64;
-
-// issue the six bf16 products D = F * X (X parts at xb) and commit them to bar
+// issue the six bf16 products D = F' * X (N = TP_N vectors) and commit them to bar
 __device__ __forceinline__ void tc_issue(unsigned char *A, unsigned char *xb, unsigned tmem, unsigned bar) {
-  constexpr unsigned IDESC = idesc_bf16(TC_M, TC_N);
+  constexpr unsigned IDESC = idesc_bf16(TC_M, TP_N);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int pa[6] = {1, 0, 2, 0, 1, 0};
   const int pb[6] = {1, 2, 0, 1, 0, 0};
   for (int t = 0; t < 6; t++) {
     const unsigned abase = smem_addr(A + pa[t] * A_BYTES);
-    const unsigned bbase = smem_addr(xb + pb[t] * B_BYTES);
+    const unsigned bbase = smem_addr(xb + pb[t] * X_BYTES);
 #pragma unroll
     for (int kk = 0; kk < TC_K / 16; kk++) {
       const unsigned long long ad = smem_desc(abase + kk * 256, 128, (TC_K / 8) * 128);
@@ -249,87 +254,77 @@ __device__ __forceinline__ void tc_issue(unsigned char *A, unsigned char *xb, un
                : "memory");
 }
 
-// TMEM result (128 lanes x 64 columns) -> stg[m][c] (row pitch DP), by 8 warps
-__device__ __forceinline__ void tmem_to_stage(unsigned tmem, float *stg, int warp, int lane) {
-  const int q4 = warp & 3, h = warp >> 2;
-  const int m = 32 * q4 + lane;
+// 32 consecutive TMEM columns of this warp's lane quadrant
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
+  unsigned r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int c = 0; c < 32; c += 8) {
-    const int c0 = 32 * h + c;
-    unsigned r[8];
-    const unsigned taddr = tmem + ((unsigned)(32 * q4) << 16) + (unsigned)c0;
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    uint4 *d4 = reinterpret_cast<uint4 *>(stg + m * DP + c0);
-    d4[0] = make_uint4(r[0], r[1], r[2], r[3]);
-    d4[1] = make_uint4(r[4], r[5], r[6], r[7]);
-  }
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// split eight complex values into the three bf16 parts of operand row `row`,
-// columns kc..kc+7 (re) and 64+kc..64+kc+7 (im)
-__device__ __forceinline__ void store_parts8(unsigned char *xb, int row, int kc, const float2 (&x)[8]) {
-  unsigned wr[3][4], wi[3][4];
+// three bf16 parts of eight consecutive K values of operand row `row` at
+// columns k0..k0+7, one 16-byte store per part
+__device__ __forceinline__ void store_parts8_row(unsigned char *xb, int row, int k0, const float *v) {
+  unsigned w[3][4];
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
-    __nv_bfloat16 r[3], im[3];
-    split3(x[q].x, r[0], r[1], r[2]);
-    split3(x[q].y, im[0], im[1], im[2]);
+  for (int q = 0; q < 8; q += 2) {
+    __nv_bfloat16 a[3], b[3];
+    split3(v[q], a[0], a[1], a[2]);
+    split3(v[q + 1], b[0], b[1], b[2]);
 #pragma unroll
-    for (int pp = 0; pp < 3; pp++) {
-      const unsigned br = __bfloat16_as_ushort(r[pp]), bi = __bfloat16_as_ushort(im[pp]);
-      if (q & 1) {
-        wr[pp][q >> 1] |= br << 16;
-        wi[pp][q >> 1] |= bi << 16;
-      } else {
-        wr[pp][q >> 1] = br;
-        wi[pp][q >> 1] = bi;
-      }
-    }
+    for (int pp = 0; pp < 3; pp++)
+      w[pp][q >> 1] = (unsigned)__bfloat16_as_ushort(a[pp]) | ((unsigned)__bfloat16_as_ushort(b[pp]) << 16);
   }
-  const int offr = kmajor_off(row, kc, TC_K), offi = kmajor_off(row, 64 + kc, TC_K);
+  const int off = kmajor_off(row, k0, TC_K);
 #pragma unroll
-  for (int pp = 0; pp < 3; pp++) {
-    *reinterpret_cast<uint4 *>(xb + pp * B_BYTES + offr) = make_uint4(wr[pp][0], wr[pp][1], wr[pp][2], wr[pp][3]);
-    *reinterpret_cast<uint4 *>(xb + pp * B_BYTES + offi) = make_uint4(wi[pp][0], wi[pp][1], wi[pp][2], wi[pp][3]);
-  }
+  for (int pp = 0; pp < 3; pp++)
+    *reinterpret_cast<uint4 *>(xb + pp * X_BYTES + off) = make_uint4(w[pp][0], w[pp][1], w[pp][2], w[pp][3]);
 }
 
-// One radix-4096 Stockham pass of an FP32 FFT as a four-step transform on the
-// tensor cores: one sub-transform per tile; with r = r1 + 64 r2 and
-// k = k2 + 64 k1,
-//   Y[r1][k2] = sum_r2 v[r1 + 64 r2] W64^(r2 k2)            (tensor cores)
-//   V[k2 + 64 k1] = sum_r1 W64^(r1 k1) W4096^(r1 k2) Y[r1][k2] (tensor cores)
-// where v[r] = in[j + r S] * w((j mod Ns) r / (Ns 4096)) and the result goes
-// to out[(j / Ns) Ns 4096 + (j mod Ns) + k Ns].
+// A first radix-4096 Stockham pass (Ns = 1) of an FP32 FFT as a four-step
+// transform on the tensor cores, two sub-transforms j, j + 1 (adjacent in
+// memory) per tile.  With r = r1 + 64 r2 and k = k2 + 64 k1:
+//   Y[r1][k2] = sum_r2 v[r1 + 64 r2] W64^(r2 k2)                   (product 1)
+//   V[k2 + 64 k1] = sum_r1 W64^(r1 k1) W4096^(r1 k2) Y[r1][k2]       (product 2)
+// where v[r] = in[j + r S] (S = N / 4096 sub-transforms per row, the sum of
+// nsum partial inputs sstride apart) and out[j 4096 + k] = V[k].
+// Product 1's X operand: row n = (jj, r1) = 64 jj + r1, column K = r2 (Re) and
+// 64 + r2 (Im).  Its result D (TMEM lane 2 k2 + c, column n) is read back
+// lane by lane: lanes 2 k2 and 2 k2 + 1 (adjacent threads of one warp) hold
+// Re and Im of Y[r1][k2], exchange them with a shuffle, apply W4096^(r1 k2)
+// and write product 2's X operand: row (jj, k2), column r1 (Re) / 64 + r1 (Im).
+// Product 2's result, lane 2 k1 + c and column (jj, k2), is V[k2 + 64 k1]:
+// each thread pair again exchanges halves so that each thread stores 32
+// consecutive outputs.
 __global__ void __launch_bounds__(TP_THREADS, 1) tc4096_pass_kernel(TcPassArgs a) {
   extern __shared__ __align__(1024) unsigned char tsm[];
-  unsigned char *A = tsm;
-  unsigned char *Bm = tsm + 3 * A_BYTES;
-  float *stg = reinterpret_cast<float *>(tsm + 3 * A_BYTES + 3 * B_BYTES);  // [128][DP]
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tsm + 3 * A_BYTES + 3 * B_BYTES + ST_BYTES);
+  unsigned char *A = tsm;                       // 3 parts of F'
+  unsigned char *X = tsm + 3 * A_BYTES;         // 3 parts of the operand of the current product
+  float2 *t4k = reinterpret_cast<float2 *>(tsm + 3 * A_BYTES + 3 * X_BYTES);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tsm + 3 * A_BYTES + 3 * X_BYTES + TW_BYTES);
   unsigned long long *fbar = bar + 1;
   unsigned *tmem_slot = reinterpret_cast<unsigned *>(bar + 2);
-  unsigned *red = tmem_slot + 1;  // [8]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quad = warp & 3, half = warp >> 2;
   const float2 *__restrict__ in = reinterpret_cast<const float2 *>(a.in);
   float2 *__restrict__ out = reinterpret_cast<float2 *>(a.out);
-  float *__restrict__ smp = reinterpret_cast<float *>(a.samples);
-  const float2 *__restrict__ thi = reinterpret_cast<const float2 *>(a.tw_hi);
-  const float2 *__restrict__ tlo = reinterpret_cast<const float2 *>(a.tw_lo);
-  const float2 *__restrict__ t4k = reinterpret_cast<const float2 *>(a.tw_R);  // exp(-2 pi i m / 4096)
+  const float2 *__restrict__ twg = reinterpret_cast<const float2 *>(a.tw_R);
   const int logS = a.logN - 12;
-  const long long Smask = (1LL << logS) - 1;
-  const int logNs = a.logNs;
-  const long long Nsmask = (1LL << logNs) - 1;
-  const int hmask = (1 << a.tw_h) - 1;
+  const long long S = 1LL << logS;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
-                 "r"(TC_N)
+                 "r"(TP_N)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -346,51 +341,73 @@ __global__ void __launch_bounds__(TP_THREADS, 1) tc4096_pass_kernel(TcPassArgs a
         "l"(a.F), "r"(3 * A_BYTES), "r"(smem_addr(fbar))
         : "memory");
   }
+  for (int i = tid; i < 4096; i += TP_THREADS) t4k[i] = twg[i];
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const unsigned tmem = *tmem_slot;
+  const unsigned tq = tmem + ((unsigned)(32 * quad) << 16);  // this warp's lane quadrant
+  const int L = 32 * quad + lane;                             // TMEM lane of this thread
+  const int kc = L >> 1, c = L & 1;                           // output index, Re (0) / Im (1)
+  const int jj = half;                                        // sub-transform of this thread's columns
   unsigned phase = 0;
   bool ok = true, f_ready = false;
+  const long long ntiles = (a.total + 1) >> 1;
 
-  for (long long u = blockIdx.x; u < a.total && ok; u += gridDim.x) {
-    const long long b = u >> logS, j = u & Smask;
+  for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const long long u0 = 2 * t;
+    const bool two = u0 + 1 < a.total;
+    const long long b = u0 >> logS, j = u0 & (S - 1);  // j even: j and j + 1 share a row
     const float2 *src = in + b * a.bstride + j;
-    // ---- step 1 operand: row r1, columns r2 (eight per item)
-    {
-      float2 xv[2][8];
+    // ---- product 1 operand: items (r1, g), r2 = 8 g + q
+#pragma unroll 1
+    for (int it = 0; it < 2; it++) {
+      const int item = tid + it * TP_THREADS;
+      const int r1 = item & 63, g = item >> 6;
+      float4 xv[8];
 #pragma unroll
-      for (int it = 0; it < 2; it++) {
-        const int item = tid + it * TP_THREADS;
-        const int r1 = item & 63, g = item >> 6;
-#pragma unroll
-        for (int q = 0; q < 8; q++) xv[it][q] = src[(long long)(r1 + 64 * (8 * g + q)) << logS];
-        // row-group partial inputs (first pass after the streaming perm+filter),
-        // added in group order
-        for (int s2 = 1; s2 < a.nsum; s2++)
-#pragma unroll
-          for (int q = 0; q < 8; q++)
-            xv[it][q] = cadd(xv[it][q], src[s2 * a.sstride + ((long long)(r1 + 64 * (8 * g + q)) << logS)]);
+      for (int q = 0; q < 8; q++) {
+        const long long off = (long long)(r1 + 64 * (8 * g + q)) << logS;
+        if (two) {
+          xv[q] = *reinterpret_cast<const float4 *>(src + off);
+        } else {
+          const float2 v = src[off];
+          xv[q] = make_float4(v.x, v.y, 0.f, 0.f);
+        }
       }
-#pragma unroll
-      for (int it = 0; it < 2; it++) {
-        const int item = tid + it * TP_THREADS;
-        const int r1 = item & 63, g = item >> 6;
+      for (int s2 = 1; s2 < a.nsum; s2++) {
 #pragma unroll
         for (int q = 0; q < 8; q++) {
-          float2 x = xv[it][q];
-          if (a.inverse) x.y = -x.y;
-          if (logNs > 0) {
-            const long long mm = (j & Nsmask) * (long long)(r1 + 64 * (8 * g + q));
-            x = cmul(x, cmul(thi[mm >> a.tw_h], tlo[mm & hmask]));
+          const long long off = s2 * a.sstride + ((long long)(r1 + 64 * (8 * g + q)) << logS);
+          float4 v;
+          if (two) {
+            v = *reinterpret_cast<const float4 *>(src + off);
+          } else {
+            const float2 w = src[off];
+            v = make_float4(w.x, w.y, 0.f, 0.f);
           }
-          xv[it][q] = x;
+          xv[q].x += v.x;
+          xv[q].y += v.y;
+          xv[q].z += v.z;
+          xv[q].w += v.w;
         }
-        store_parts8(Bm, r1, 8 * g, xv[it]);
       }
+      float re0[8], im0[8], re1[8], im1[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        re0[q] = xv[q].x;
+        im0[q] = a.inverse ? -xv[q].y : xv[q].y;
+        re1[q] = xv[q].z;
+        im1[q] = a.inverse ? -xv[q].w : xv[q].w;
+      }
+      store_parts8_row(X, r1, 8 * g, re0);
+      store_parts8_row(X, r1, 64 + 8 * g, im0);
+      store_parts8_row(X, 64 + r1, 8 * g, re1);
+      store_parts8_row(X, 64 + r1, 64 + 8 * g, im1);
     }
     for (int step = 0; step < 2 && ok; step++) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       if (tid == 0) {
         bool go = true;
@@ -399,11 +416,10 @@ __global__ void __launch_bounds__(TP_THREADS, 1) tc4096_pass_kernel(TcPassArgs a
           f_ready = go;
         }
         if (go) {
-          tc_issue(A, Bm, tmem, smem_addr(bar));
+          tc_issue(A, X, tmem, smem_addr(bar));
         } else {
-          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                           smem_addr(bar))
-                       : "memory");
+          // nothing issued: arrive on the barrier so that every thread leaves its wait
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
           ok = false;
           if (a.err) atomicExch(a.err, 1);
         }
@@ -412,70 +428,60 @@ __global__ void __launch_bounds__(TP_THREADS, 1) tc4096_pass_kernel(TcPassArgs a
         ok = false;
         if (tid == 0 && a.err) atomicExch(a.err, 1);
       }
-      ok = __syncthreads_and(ok) != 0;
+      ok = __syncthreads_and(ok) != 0;  // warp-collective TMEM loads below: all or none
       phase ^= 1u;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (!ok) break;
-      tmem_to_stage(tmem, stg, warp, lane);  // stg[m][c]: m = output (re | im), c = vector
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
       if (step == 0) {
-        // step 3 operand: row k2, columns r1: Z = Y[r1][k2] * W4096^(r1 k2)
+        // D1 lane (kc = k2, c), columns n = 64 jj + r1  ->  product 2 operand
+#pragma unroll 1
+        for (int c0 = 0; c0 < 64; c0 += 32) {
+          float y[32];
+          tmem_ld32(tq + (unsigned)(64 * jj + c0), y);
+          float z[32];
 #pragma unroll
-        for (int it = 0; it < 2; it++) {
-          const int item = tid + it * TP_THREADS;
-          const int k2 = item & 63, g = item >> 6;
-          float2 z[8];
-#pragma unroll
-          for (int q = 0; q < 8; q++) {
-            const int r1 = 8 * g + q;
-            const float2 y = make_float2(stg[k2 * DP + r1], stg[(64 + k2) * DP + r1]);
-            z[q] = cmul(y, __ldg(&t4k[(r1 * k2) & 4095]));
+          for (int i = 0; i < 32; i++) {
+            const float other = __shfl_xor_sync(0xffffffffu, y[i], 1);
+            const float yr = c ? other : y[i], yi = c ? y[i] : other;
+            const float2 w = t4k[((c0 + i) * kc) & 4095];
+            z[i] = c ? fmaf(yr, w.y, yi * w.x) : fmaf(yr, w.x, -(yi * w.y));
           }
-          store_parts8(Bm, k2, 8 * g, z);
-        }
-      }
-    }
-    if (!ok) break;
-    // ---- outputs: k = k2 + 64 k1; stg[k1 (re) | 64 + k1 (im)][k2]
-    float tmax = 0.f;
-#pragma unroll 4
-    for (int e = tid; e < 4096; e += TP_THREADS) {
-      const int k2 = e & 63, k1 = e >> 6;
-      const int k = k2 + 64 * k1;
-      const float re = stg[k1 * DP + k2];
-      float im = stg[(64 + k1) * DP + k2];
-      if (a.inverse) im = -im;
-      const long long dest = b * a.bstride + ((j >> logNs) << (logNs + 12)) + (j & Nsmask) +
-                             ((long long)k << logNs);
-      if (a.write_complex) out[dest] = make_float2(re, im);
-      if (smp) {
-        const float sq = __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
-        smp[dest] = sq;
-        tmax = sq > tmax ? sq : tmax;
-      }
-    }
-    if (smp && a.row_max) {
-      unsigned kmax = __float_as_uint(tmax);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned y = __shfl_xor_sync(0xffffffffu, kmax, o);
-        kmax = y > kmax ? y : kmax;
-      }
-      if (lane == 0) red[warp] = kmax;
-      __syncthreads();
-      if (tid == 0) {
-        unsigned m8 = red[0];
-        for (int w2 = 1; w2 < TP_THREADS / 32; w2++) m8 = red[w2] > m8 ? red[w2] : m8;
-        atomicMax(reinterpret_cast<unsigned *>(a.row_max) + b, m8);
+          for (int grp = 0; grp < 4; grp++)
+            store_parts8_row(X, 64 * jj + kc, (c ? 64 : 0) + c0 + 8 * grp, z + 8 * grp);
+        }
+      } else if (jj == 0 || two) {
+        // D3 lane (kc = k1, c), columns (jj, k2): V[k2 + 64 k1]; this thread keeps k2 in [32 c, 32 c + 32)
+        float2 v[32];
+#pragma unroll 1
+        for (int c0 = 0; c0 < 64; c0 += 32) {
+          float y[32];
+          tmem_ld32(tq + (unsigned)(64 * jj + c0), y);
+          const bool keep = c0 == 32 * c;
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            const float other = __shfl_xor_sync(0xffffffffu, y[i], 1);
+            if (keep) v[i] = c ? make_float2(other, y[i]) : make_float2(y[i], other);
+          }
+        }
+        float2 *dp = out + b * a.bstride + (j + jj) * 4096 + 64 * kc + 32 * c;
+#pragma unroll
+        for (int i = 0; i < 32; i += 2) {
+          const float s = a.inverse ? -1.f : 1.f;
+          *reinterpret_cast<float4 *>(dp + i) = make_float4(v[i].x, s * v[i].y, v[i + 1].x, s * v[i + 1].y);
+        }
+      } else {
+        // the second sub-transform of a tile with one: no outputs, but the
+        // warp still took part in the collective loads of the other half
       }
     }
-    __syncthreads();  // the staging and operand buffers are rewritten by the next tile
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // the operand buffer and TMEM are rewritten by the next tile
   }
   if (tid == 0 && !f_ready) (void)mbar_wait_bounded(smem_addr(fbar), 0);
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP_N) : "memory");
 }
 
 }  // namespace
@@ -509,6 +515,13 @@ int tc_build_F(void **F) {
 }
 
 int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st) {
+  // first passes only (Ns = 1, outputs contiguous per sub-transform), an even
+  // number of sub-transforms per row and 16-byte aligned element pairs
+  if (a.logNs != 0 || a.logN < 13 || !a.tw_R || !a.F || a.samples || a.row_max || !a.write_complex)
+    return GSFFT_ERR_UNSUPPORTED;
+  if ((reinterpret_cast<uintptr_t>(a.in) & 15) || (reinterpret_cast<uintptr_t>(a.out) & 15) ||
+      (a.bstride & 1) || (a.nsum > 1 && (a.sstride & 1)))
+    return GSFFT_ERR_UNSUPPORTED;
   static PerContext<int> attr;  // the kernel's dynamic shared memory limit, per context
   GS_CHECK(attr.ensure_at_least(TC4K_SMEM, [](int v) {
     if (cudaFuncSetAttribute(tc4096_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v) ==
@@ -518,16 +531,15 @@ int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st) {
                    cudaGetErrorString(cudaGetLastError()));
     return (int)GSFFT_ERR_CUDA;
   }));
-  if (a.logN < 12 || !a.tw_R) return GSFFT_ERR_UNSUPPORTED;
   int dev = 0, sms = 0;
   GS_CUDA(cudaGetDevice(&dev));
   GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int grid = (int)(a.total < sms ? a.total : sms);
+  const long long ntiles = (a.total + 1) / 2;
+  const int grid = (int)(ntiles < sms ? ntiles : sms);
   if (grid < 1) return GSFFT_OK;
   tc4096_pass_kernel<<<grid, TP_THREADS, TC4K_SMEM, st>>>(a);
   GS_LAUNCHED();
   return GSFFT_OK;
 }
-
 
 }  // namespace gsfft

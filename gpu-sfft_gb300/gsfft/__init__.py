@@ -25,6 +25,7 @@ FLAG_RAW_SELECTION = 2
 FLAG_FORCE_GATHER = 4
 FLAG_FORCE_STREAM = 8
 FLAG_TC_BUCKET_FFT = 16
+FLAG_TC_RLFC_FFT = 32
 SELECTION_FLOOR = 1e-10
 OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE = range(7)
 
@@ -101,6 +102,7 @@ def lib():
         "gsfft_plan_stage_times": ([P, C.POINTER(C.c_float), i, C.POINTER(i)], i),
         "gsfft_stage_name": ([i], C.c_char_p),
         "gsfft_fft": ([P, P, ll, i, i, i, P], i),
+        "gsfft_fft_tc": ([P, P, ll, i, i, P], i),
         "gsfft_cutoff": ([P, i, i, i, i, P, P], i),
         "gsfft_cutoff_noalloc": ([P, i, i, i, i, P, P], i),
         "gsfft_cutoff_floor": ([P, i, i, i, i, d, P, P, P], i),
@@ -170,6 +172,11 @@ def design_filter(p, d_filter_time, d_filter_freq=0, stream=0):
 
 def fft(d_in, d_out, n, batch=1, sign=-1, precision=FP64, stream=0):
     check(lib().gsfft_fft(d_in, d_out, n, batch, sign, precision, stream or None), "gsfft_fft")
+
+
+def fft_tc(d_in, d_out, n, batch=1, sign=-1, stream=0):
+    """FP32 FFT with the tensor-core radix-4096 first pass (n = 2^17 .. 2^26)."""
+    check(lib().gsfft_fft_tc(d_in, d_out, n, batch, sign, stream or None), "gsfft_fft_tc")
 
 
 def cutoff(d_samples, size, num, batch, precision, d_out, stream=0):

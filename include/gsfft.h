@@ -66,6 +66,10 @@ typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
    radix-2^(L-12) pass and a 4096-point four-step pass whose two DFT_64 stages
    run on the tensor cores (tcgen05, three-part bf16 split products
    accumulated in fp32), when B = 2^L with 17 <= L <= 26 */
+#define GSFFT_FLAG_TC_RLFC_FFT 32u   /* MIXED: the same tensor-core radix-4096 first
+   pass for the W_RLFC-point RLFC FFT, when W_RLFC = 2^L with 17 <= L <= 26 and
+   the plan uses the streaming perm+filter (which writes the sub-samples the
+   transform reads) */
 
 /* Run parameters derived exactly as experiment.c:71-84 and
  * cuExperiment.cu:279-284 derive them. */
@@ -223,6 +227,16 @@ int gsfft_evaluate(gsfft_plan plan, const complex_t *d_x_f, const int *d_true_lo
  * complex_t or {float, float} elements. */
 int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
               int precision, void *stream);
+
+/* The FP32 FFT of the mixed path's tensor-core plans: batch unnormalised
+ * complex FFTs of n_fft = 2^L points, 17 <= L <= 26, {float, float} elements,
+ * whose first pass (radix 4096 = 64 x 64, both DFT_64 stages as tcgen05
+ * products of three-part bf16 splits accumulated in fp32) runs on the tensor
+ * cores and whose second pass (radix 2^(L-12)) on the CUDA cores; sign -1
+ * forward, +1 inverse.  Replaces cuFFT's C2C plans of the reference's bucket
+ * and RLFC transforms (innerLoop.cu:144-152, :252-256) in single precision. */
+int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
+                 void *stream);
 
 /* Tensor-core building block of the mixed bucket FFT (the DFT stages that
  * replace cuFFT's B-point transform, innerLoop.cu:247-262): nvec independent

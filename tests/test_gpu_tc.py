@@ -60,3 +60,21 @@ def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
     a = np.array([v64[kk] for kk in k64.tolist()])
     b = np.array([vtc[kk] for kk in k64.tolist()])
     assert np.linalg.norm(a - b) / np.linalg.norm(a) <= 1e-5
+
+
+@pytest.mark.parametrize("n,batch,sign", [(1 << 17, 9, -1), (1 << 20, 2, -1), (1 << 22, 2, -1),
+                                          (1 << 17, 1, 1)])
+def test_tc_fft_matches_numpy(G, torch_cuda, n, batch, sign):
+    """The FP32 FFT whose radix-4096 first pass runs on the tensor cores (the
+    bucket FFT's B = 2^17 shape and the RLFC FFT's W = 2^22 shape)."""
+    torch = torch_cuda
+    rng = np.random.default_rng(n + batch)
+    x = (rng.normal(size=(batch, n)) + 1j * rng.normal(size=(batch, n))).astype(np.complex64)
+    d_x = torch.from_numpy(x).cuda()
+    d_y = torch.zeros_like(d_x)
+    G.fft_tc(d_x.data_ptr(), d_y.data_ptr(), n, batch, sign)
+    got = d_y.cpu().numpy().astype(np.complex128)
+    x64 = x.astype(np.complex128)
+    want = np.fft.fft(x64, axis=1) if sign < 0 else np.fft.ifft(x64, axis=1) * n
+    err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    assert err.max() < 2e-6, err.max()
