@@ -158,10 +158,21 @@ int gsfft_design_filter(const gsfft_params *p, complex_t *d_filter_time, complex
 
 int gsfft_plan_create(const gsfft_params *p, int precision, unsigned flags, int max_candidates,
                       gsfft_plan *out) {
+  return gsfft_plan_create_tuned(p, precision, flags, max_candidates, nullptr, out);
+}
+
+int gsfft_plan_get_tuning(gsfft_plan plan, gsfft_plan_tuning *out) {
+  if (!plan || !out) return GSFFT_ERR_PARAM;
+  *out = plan->impl->tuning;
+  return GSFFT_OK;
+}
+
+int gsfft_plan_create_tuned(const gsfft_params *p, int precision, unsigned flags,
+                            int max_candidates, const gsfft_plan_tuning *t, gsfft_plan *out) {
   if (!p || !out) return GSFFT_ERR_PARAM;
   *out = nullptr;
   Plan *impl = nullptr;
-  int s = plan_create(*p, precision, flags, max_candidates, &impl);
+  int s = plan_create(*p, precision, flags, max_candidates, &impl, t);
   if (s != GSFFT_OK) return s;
   gsfft_plan h = (gsfft_plan)malloc(sizeof(gsfft_plan_s));
   if (!h) {

@@ -92,10 +92,18 @@ int validate_params(const gsfft_params &p) {
 }
 
 int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_candidates,
-                Plan **out) {
+                Plan **out, const gsfft_plan_tuning *tuning) {
   *out = nullptr;
   GS_CHECK(validate_params(pp));
   if (precision != GSFFT_FP64 && precision != GSFFT_MIXED) return GSFFT_ERR_PARAM;
+  gsfft_plan_tuning tn = {};
+  if (tuning) tn = *tuning;
+  if (tn.perm_filter_form < 0 || tn.perm_filter_form > 2 || tn.select_form < 0 ||
+      tn.select_form > 2 || tn.row_groups < 0 || tn.bucket_first_radix < 0 ||
+      tn.rlfc_first_radix < 0)
+    return GSFFT_ERR_PARAM;
+  if (tn.perm_filter_form == 1) flags = (flags | GSFFT_FLAG_FORCE_STREAM) & ~GSFFT_FLAG_FORCE_GATHER;
+  if (tn.perm_filter_form == 2) flags = (flags | GSFFT_FLAG_FORCE_GATHER) & ~GSFFT_FLAG_FORCE_STREAM;
   Plan *P = new Plan();
   P->p = pp;
   P->precision = precision;
@@ -142,8 +150,19 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
                     ((flags & GSFFT_FLAG_FORCE_STREAM) ||
                      (precision == GSFFT_MIXED && stream_bytes < gather_bytes));
   }
+  if (tn.perm_filter_form == 1 && !P->use_stream) {
+    plan_destroy(P);
+    return GSFFT_ERR_PARAM;  // the ordered pass does not support these sizes
+  }
   if (P->use_stream) {
     P->groups = stream_pf_groups(p.n, p.B, p.w, p.loops, precision);
+    if (tn.row_groups > 0) {
+      if (!stream_pf_groups_valid(p.n, p.B, tn.row_groups, precision)) {
+        plan_destroy(P);
+        return GSFFT_ERR_PARAM;
+      }
+      P->groups = tn.row_groups;
+    }
     A(ybuf, V * (size_t)p.RLFC_loops * p.W_RLFC);
     A(bpart, V * (size_t)P->groups * p.loops * p.B);
     A(filt_bm, V * (size_t)stream_taps_count(p.w, p.B));
@@ -155,7 +174,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
     if (precision == GSFFT_MIXED && (flags & GSFFT_FLAG_TC_BUCKET_FFT))
       t = fft_plan_init_tc(P->fftB, p.B, p.loops);
     P->tc_bucket = t == GSFFT_OK;
-    if (!P->tc_bucket) s = fft_plan_init(P->fftB, p.B, precision, p.loops);
+    if (!P->tc_bucket) s = fft_plan_init(P->fftB, p.B, precision, p.loops, tn.bucket_first_radix);
   }
   if (s == GSFFT_OK) {
     // the RLFC transform reads the streaming pass's sub-samples; its first
@@ -165,11 +184,19 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
     if (precision == GSFFT_MIXED && (flags & GSFFT_FLAG_TC_RLFC_FFT) && P->use_stream)
       t = fft_plan_init_tc(P->fftW, p.W_RLFC, p.RLFC_loops);
     P->tc_rlfc = t == GSFFT_OK;
-    if (!P->tc_rlfc) s = fft_plan_init(P->fftW, p.W_RLFC, precision, p.RLFC_loops);
+    if (!P->tc_rlfc)
+      s = fft_plan_init(P->fftW, p.W_RLFC, precision, p.RLFC_loops, tn.rlfc_first_radix);
   }
   if (s == GSFFT_OK) s = select_scratch_init(P->selB, p.loops_loc, p.B);
   if (s == GSFFT_OK) s = select_scratch_init(P->selW, p.RLFC_loops, p.W_RLFC);
   if (s == GSFFT_OK) s = select_scratch_init(P->selK, 1, P->cap);
+  P->selB.single_launch = P->selW.single_launch = P->selK.single_launch = tn.select_form != 2;
+  // record the shapes in use
+  P->tuning.perm_filter_form = P->use_stream ? 1 : 2;
+  P->tuning.row_groups = P->use_stream ? P->groups : 0;
+  P->tuning.bucket_first_radix = P->fftB.npass == 2 && !P->tc_bucket ? P->fftB.logR[0] : 0;
+  P->tuning.rlfc_first_radix = P->fftW.npass == 2 && !P->tc_rlfc ? P->fftW.logR[0] : 0;
+  P->tuning.select_form = tn.select_form == 2 ? 2 : 1;
   if (s == GSFFT_OK &&
       (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess ||
        cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -305,7 +332,8 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   BEGIN(ST_PERM_FILTER);
   if (P->use_stream)
     GS_CHECK(launch_perm_filter_stream(P->precision, d_x, p.n, P->filt_bm, p.w, p.B, p.loops, d,
-                                       P->bpart, p.RLFC_loops, P->ybuf, p.W_RLFC, &P->ctl->err, st));
+                                       P->bpart, p.RLFC_loops, P->ybuf, p.W_RLFC, &P->ctl->err, st,
+                                       P->groups));
   else
     GS_CHECK(launch_perm_filter(P->precision, d_x, p.n, P->filt, p.w, p.B, p.loops, d, quirk,
                                 P->bins, st));

@@ -47,6 +47,7 @@ struct Plan {
   bool tc_bucket = false;  // bucket FFT with tensor-core passes
   bool tc_rlfc = false;    // RLFC FFT with a tensor-core first pass
   double floor_rel = 1e-10;
+  gsfft_plan_tuning tuning = {};  // the stage shapes in use (rules' choices filled in)
   // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
   // side stream of the bucket FFT and cutoff (they need only the perm+filter)
   cudaStream_t side = nullptr;
@@ -58,7 +59,7 @@ struct Plan {
 
 int validate_params(const gsfft_params &p);
 int plan_create(const gsfft_params &p, int precision, unsigned flags, int max_candidates,
-                Plan **out);
+                Plan **out, const gsfft_plan_tuning *tuning = nullptr);
 void plan_destroy(Plan *P);
 int plan_set_filter(Plan *P, const void *d_filter_time, const void *d_filter_freq,
                     cudaStream_t st);

@@ -37,7 +37,7 @@ int dispatch_pass(bool dbl, int logr, const PassArgs &a, long long total_sub, cu
 
 }  // namespace
 
-int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch) {
+int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch, int first_logr) {
   fft_plan_free(p);
   if (n < 256 || (n & (n - 1)) != 0) return GSFFT_ERR_UNSUPPORTED;
   int L = 0;
@@ -47,13 +47,21 @@ int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch) {
   p.L = L;
   p.precision = precision;
   if (L <= one_pass_max) {
+    if (first_logr > 0) return GSFFT_ERR_PARAM;  // one pass: no first radix to choose
     p.npass = 1;
     p.logR[0] = L;
   } else if (L <= 24) {
     p.npass = 2;
     p.logR[0] = (L + 1) / 2;
+    if (first_logr > 0) {
+      if (first_logr < 7 || first_logr > one_pass_max || L - first_logr < 7 ||
+          L - first_logr > one_pass_max)
+        return GSFFT_ERR_PARAM;
+      p.logR[0] = first_logr;
+    }
     p.logR[1] = L - p.logR[0];
   } else if (L <= 36) {
+    if (first_logr > 0) return GSFFT_ERR_PARAM;
     p.npass = 3;
     p.logR[0] = (L + 2) / 3;
     p.logR[1] = (L - p.logR[0] + 1) / 2;

@@ -225,7 +225,8 @@ struct FftIo {
   int *err = nullptr;
 };
 
-int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch);
+// first_logr: log2 of the first pass's radix for two-pass sizes (0: ceil(L/2))
+int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch, int first_logr = 0);
 // FP32 plan: radix-4096 tensor-core pass, then a CUDA-core pass of radix
 // n / 4096; GSFFT_ERR_UNSUPPORTED unless n = 2^(17..26)
 int fft_plan_init_tc(FftPlan &p, long long n, int max_batch);
@@ -247,6 +248,7 @@ struct SelectScratch {
   void *tiles = nullptr;       // batch * max_tiles * 4 uint32
   void *coop_hist = nullptr;   // single-launch form: 6 passes x 8 rows x 2048 bins, zero between calls
   int max_batch = 0, max_tiles = 0;
+  bool single_launch = true;   // cluster / cooperative form allowed (else multi-launch)
 };
 extern bool g_select_coop;  // use the single-launch select (cluster or cooperative form)
 // Byte sizes of the SelectScratch regions for max_batch rows of at most

@@ -605,9 +605,16 @@ int stream_pf_groups(int n, int B, int w, int loops, int precision) {
   return groups;
 }
 
+bool stream_pf_groups_valid(int n, int B, int groups, int precision) {
+  if (groups < 1 || (groups & (groups - 1))) return false;
+  if (groups == 1) return true;
+  const int nb = n / B;
+  return nb / groups >= 4 * stream_rows_per_tile(n, B, precision) && nb % groups == 0;
+}
+
 int launch_perm_filter_stream(int precision, const void *x, int n, const void *filt, int w, int B,
                               int loops, const Draws &d, void *bins, int nrlfc, void *y, int W,
-                              int *err, cudaStream_t st) {
+                              int *err, cudaStream_t st, int groups_req) {
   if (!stream_pf_supported(n, B, loops, W, nrlfc)) return GSFFT_ERR_UNSUPPORTED;
   const int tiles = w / B;
   if (tiles >= MAXT || tiles > 255) return GSFFT_ERR_UNSUPPORTED;
@@ -631,7 +638,11 @@ int launch_perm_filter_stream(int precision, const void *x, int n, const void *f
   const bool dbl = precision == GSFFT_FP64;
   const int es = dbl ? 16 : 8;
   const int rt = stream_rows_per_tile(n, B, precision);
-  const int groups = stream_pf_groups(n, B, w, loops, precision);
+  int groups = stream_pf_groups(n, B, w, loops, precision);
+  if (groups_req > 0) {
+    if (!stream_pf_groups_valid(n, B, groups_req, precision)) return GSFFT_ERR_PARAM;
+    groups = groups_req;
+  }
   const int cw = cols_per_item(loops);
   CUtensorMap tm;
   const cuuint64_t gdim[2] = {(cuuint64_t)B * (es / 8), (cuuint64_t)nb};

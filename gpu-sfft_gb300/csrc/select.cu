@@ -949,7 +949,7 @@ int select_top(const void *keys, int key_bytes, long long size, const int *size_
                int batch, long long row_stride, int *out, long long out_stride, int *count_out,
                SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
   if (size_dev && batch != 1) return GSFFT_ERR_PARAM;
-  if (g_select_coop && batch <= MAXB && batch <= s.max_batch &&
+  if (g_select_coop && s.single_launch && batch <= MAXB && batch <= s.max_batch &&
       (size + SEL_TILE - 1) / SEL_TILE <= s.max_tiles) {
     for (const bool clu : {true, false}) {
       if (clu && !(size <= CLUSTER_ROW_MAX || size_dev)) continue;

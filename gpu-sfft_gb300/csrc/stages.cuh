@@ -50,9 +50,13 @@ int launch_sum_partials(int precision, const void *part, int groups, long long c
 int stream_taps_count(int w, int B);
 int launch_stream_taps(int precision, const void *filt, int w, int B, void *taps_bm, cudaStream_t st);
 // filt here is the bucket-major table
+// groups: row groups (partial bin sets) of the pass; 0 = stream_pf_groups
 int launch_perm_filter_stream(int precision, const void *x, int n, const void *filt, int w, int B,
                               int loops, const Draws &d, void *bins, int nrlfc, void *y, int W,
-                              int *err, cudaStream_t st);
+                              int *err, cudaStream_t st, int groups = 0);
+// whether `groups` row groups suit the streaming pass at this shape (one, or
+// a power of two leaving at least four tiles of rows per group)
+bool stream_pf_groups_valid(int n, int B, int groups, int precision);
 
 // J2 = sorted distinct union of the RLFC blocks, through a W-bit bitmap.
 int launch_j2_merge(const int *J2_blocks, int total, int W, unsigned *bitmap, int *J2,

@@ -49,6 +49,15 @@ class Params(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class Tuning(C.Structure):
+    """gsfft_plan_tuning: stage shapes of a plan (0 = the plan's rule)."""
+    _fields_ = [(f, C.c_int) for f in ("perm_filter_form", "row_groups", "bucket_first_radix",
+                                      "rlfc_first_radix", "select_form")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -77,6 +86,10 @@ def lib():
         "gsfft_derive_params": ([i, i, d, i, i, i, d, i, d, C.POINTER(Params)], i),
         "gsfft_design_filter": ([C.POINTER(Params), P, P, P], i),
         "gsfft_plan_create": ([C.POINTER(Params), i, u, i, C.POINTER(P)], i),
+        "gsfft_plan_create_tuned": ([C.POINTER(Params), i, u, i, C.POINTER(Tuning), C.POINTER(P)], i),
+        "gsfft_plan_get_tuning": ([P, C.POINTER(Tuning)], i),
+        "gsfft_autotune_plan": ([C.POINTER(Params), i, u, P, P, P, P, P, P, i, C.c_char_p,
+                                 C.POINTER(Tuning), C.POINTER(C.c_float), P], i),
         "gsfft_plan_destroy": ([P], i),
         "gsfft_plan_set_filter": ([P, P, P, P], i),
         "gsfft_run": ([P, P, P, P, P, P], i),
@@ -303,16 +316,35 @@ def stage_estimate(precision, d_cand, num, d_bins, loops, n, B, ai, d_filter_fre
                                      d_filter_freq, d_out, stream or None), "gsfft_stage_estimate")
 
 
+def autotune_plan(params, precision, flags, d_x, d_filter_time, d_filter_freq, offsets, a, ai,
+                  reps=5, cache_path=None, stream=0):
+    """gsfft_autotune_plan: the fastest stage shapes for plans of these
+    parameters, timed on this signal, filter and draws.  Returns (Tuning, ms)."""
+    o, aa, ii = [np.ascontiguousarray(v, np.int32) for v in (offsets, a, ai)]
+    t, ms = Tuning(), C.c_float(0.0)
+    check(lib().gsfft_autotune_plan(C.byref(params), precision, flags, d_x, d_filter_time,
+                                    d_filter_freq, _np_ptr(o), _np_ptr(aa), _np_ptr(ii), reps,
+                                    cache_path.encode() if cache_path else None, C.byref(t),
+                                    C.byref(ms), stream or None), "gsfft_autotune_plan")
+    return t, ms.value
+
+
 class Plan:
     """One reusable sparse-FFT plan (all device buffers allocated here)."""
 
-    def __init__(self, params, precision=FP64, flags=0, max_candidates=0):
+    def __init__(self, params, precision=FP64, flags=0, max_candidates=0, tuning=None):
         self.params = params
         self.precision = precision
         h = C.c_void_p()
-        check(lib().gsfft_plan_create(C.byref(params), precision, flags, max_candidates,
-                                      C.byref(h)), "gsfft_plan_create")
+        check(lib().gsfft_plan_create_tuned(C.byref(params), precision, flags, max_candidates,
+                                            C.byref(tuning) if tuning is not None else None,
+                                            C.byref(h)), "gsfft_plan_create_tuned")
         self.h = h
+
+    def tuning(self):
+        t = Tuning()
+        check(lib().gsfft_plan_get_tuning(self.h, C.byref(t)), "gsfft_plan_get_tuning")
+        return t
 
     def close(self):
         if self.h:

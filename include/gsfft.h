@@ -105,6 +105,41 @@ typedef struct gsfft_plan_s *gsfft_plan;
  * (utils.h:40, 524288). */
 int gsfft_plan_create(const gsfft_params *p, int precision, unsigned flags,
                       int max_candidates, gsfft_plan *out);
+
+/* Stage shapes of a plan that gsfft_plan_create otherwise picks by fixed
+ * rules; zero in a field keeps the rule.  gsfft_autotune_plan chooses them by
+ * timing. */
+typedef struct {
+  int perm_filter_form;    /* 1: one ordered pass over the signal, 2: gathers */
+  int row_groups;          /* ordered pass: row groups of the signal matrix, each
+                              with its own partial bins (power of two) */
+  int bucket_first_radix;  /* log2 of the bucket FFT's first-pass radix (two-pass sizes) */
+  int rlfc_first_radix;    /* log2 of the RLFC FFT's first-pass radix (two-pass sizes) */
+  int select_form;         /* 1: single-launch cutoffs (cluster or cooperative),
+                              2: multi-launch radix passes */
+} gsfft_plan_tuning;
+
+/* gsfft_plan_create with explicit stage shapes (t may be NULL).  Returns
+ * GSFFT_ERR_PARAM for a shape the plan's sizes cannot take. */
+int gsfft_plan_create_tuned(const gsfft_params *p, int precision, unsigned flags,
+                            int max_candidates, const gsfft_plan_tuning *t, gsfft_plan *out);
+/* The stage shapes a plan uses (the rules' choices filled in). */
+int gsfft_plan_get_tuning(gsfft_plan plan, gsfft_plan_tuning *out);
+
+/* Autotuner.  Times candidate stage shapes for plans of these parameters on
+ * the caller's signal, filter and draws (coordinate descent: perm+filter form
+ * and row groups, then each FFT's first-pass radix, then the cutoff form;
+ * each candidate the mean of `reps` runs after one warm-up run, CUDA events
+ * on `stream`) and returns the fastest in *best, with its time in *best_ms.
+ * cache_path (may be NULL): a text file of earlier results, keyed by the
+ * device, the precision, the tensor-core flags and the plan's sizes; a hit
+ * returns at once, a new result is appended.  Allocates and frees candidate
+ * plans; synchronises the stream. */
+int gsfft_autotune_plan(const gsfft_params *p, int precision, unsigned flags, const void *d_x,
+                        const complex_t *d_filter_time, const complex_t *d_filter_freq,
+                        const int *h_rlfc_offsets, const int *h_a, const int *h_ai, int reps,
+                        const char *cache_path, gsfft_plan_tuning *best, float *best_ms,
+                        void *stream);
 int gsfft_plan_destroy(gsfft_plan plan);
 
 /* Installs the filter: w time taps and the full n-bin response (only the
