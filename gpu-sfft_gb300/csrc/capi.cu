@@ -101,6 +101,7 @@ const char *gsfft_status_string(int status) {
     case GSFFT_ERR_CUDA: return "CUDA error";
     case GSFFT_ERR_UNSUPPORTED: return "unsupported size or mode";
     case GSFFT_ERR_STATE: return "invalid plan state";
+    case GSFFT_ERR_TIMEOUT: return "a bounded device-side wait gave up";
     default: return "unknown status";
   }
 }
@@ -385,6 +386,28 @@ int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sig
   return s;
 }
 
+int gsfft_check_bounded_wait(long long limit_cycles, void *stream) {
+  if (limit_cycles < 1 || limit_cycles > (1LL << 31)) return GSFFT_ERR_PARAM;
+  int *flag = nullptr;
+  if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) return GSFFT_ERR_ALLOC;
+  int s = cudaMemsetAsync(flag, 0, sizeof(int), S(stream)) == cudaSuccess ? GSFFT_OK : GSFFT_ERR_CUDA;
+  if (s == GSFFT_OK) s = launch_bounded_wait_probe(limit_cycles, flag, S(stream));
+  int gave_up = 0;
+  if (s == GSFFT_OK &&
+      (cudaMemcpyAsync(&gave_up, flag, sizeof(int), cudaMemcpyDeviceToHost, S(stream)) != cudaSuccess ||
+       cudaStreamSynchronize(S(stream)) != cudaSuccess)) {
+    set_last_error("gsfft_check_bounded_wait: %s", cudaGetErrorString(cudaGetLastError()));
+    s = GSFFT_ERR_CUDA;
+  }
+  cudaFree(flag);
+  if (s != GSFFT_OK) return s;
+  if (gave_up) {
+    set_last_error("bounded wait gave up after %lld cycles", limit_cycles);
+    return GSFFT_ERR_TIMEOUT;
+  }
+  return GSFFT_OK;
+}
+
 int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
                  void *stream) {
   if (!d_in || !d_out || batch < 1 || (sign != 1 && sign != -1)) return GSFFT_ERR_PARAM;
@@ -408,7 +431,7 @@ int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int 
       }
       if (s == GSFFT_OK && h) {
         set_last_error("gsfft_fft_tc: a tensor-core completion wait timed out");
-        s = GSFFT_ERR_CUDA;
+        s = GSFFT_ERR_TIMEOUT;
       }
       cudaFree(err);
     }

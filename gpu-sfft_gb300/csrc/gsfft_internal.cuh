@@ -109,6 +109,30 @@ extern thread_local int g_launch_counter;
     }                                                                         \
   } while (0)
 
+// ---------------------------------------------------------------- bounded waits
+// Every wait of a kernel on an mbarrier (a TMA copy's or a tensor-core
+// product's completion) gives up after `limit` SM clock cycles -- by default
+// 2^30, about half a second at 2 GHz, far above any real completion -- and
+// returns false, so that a kernel whose producer never arrives records an
+// error and returns instead of hanging the GPU.
+constexpr long long kWaitLimitCycles = 1LL << 30;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar_smem_addr, unsigned parity,
+                                                  long long limit = kWaitLimitCycles) {
+  const long long t0 = clock64();
+  while (true) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(bar_smem_addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > limit) return false;
+  }
+}
+// launches the failure-detection self-check kernel (capi.cu: gsfft_check_bounded_wait)
+int launch_bounded_wait_probe(long long limit, int *gave_up, cudaStream_t st);
+
 // ---------------------------------------------------------------- launches
 // Programmatic dependent launch.  The kernels of a run begin with pdl_enter():
 // griddepcontrol.wait returns once the preceding grid of the stream has

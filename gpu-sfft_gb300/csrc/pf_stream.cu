@@ -138,17 +138,7 @@ __device__ __forceinline__ double2 ld_tap(const double2 *p, unsigned long long p
 
 // Bounded wait on an mbarrier phase; false after ~0.5 s without completion.
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-  const long long t0 = clock64();
-  while (true) {
-    unsigned done;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (clock64() - t0 > (1LL << 30)) return false;
-  }
+  return mbar_wait_bounded(smem_u32(bar), parity);
 }
 
 // Persistent, warp-specialised.  A work item is (block of CW columns, row

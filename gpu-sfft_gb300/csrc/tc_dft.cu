@@ -63,19 +63,6 @@ __device__ __forceinline__ void split3(float v, __nv_bfloat16 &p0, __nv_bfloat16
   p2 = __float2bfloat16_rn(r2);
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
-  const long long t0 = clock64();
-  while (true) {
-    unsigned done;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (clock64() - t0 > (1LL << 30)) return false;
-  }
-}
 
 // y[v] = DFT_64(x[v]) (forward, unnormalised) for v < nvec; float2 vectors.
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -503,6 +490,28 @@ int launch_tc_dft64(const void *x, void *y, int nvec, int *err, cudaStream_t st)
   const int grid = tiles < sms ? tiles : sms;
   if (grid < 1) return GSFFT_OK;
   tc_dft64_kernel<<<grid, TC_THREADS, TC_SMEM, st>>>((const float2 *)x, (float2 *)y, nvec, err);
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+namespace {
+// Failure-detection self-check: one CTA waits on an mbarrier that nothing
+// arrives on (no copy or product is ever issued against it), with the
+// engine's bounded wait, and records that the wait gave up.
+__global__ void bounded_wait_probe_kernel(long long limit, int *gave_up) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool done = mbar_wait_bounded(smem_addr(&bar), 0, limit);
+  if (threadIdx.x == 0) *gave_up = done ? 0 : 1;
+}
+}  // namespace
+
+int launch_bounded_wait_probe(long long limit, int *gave_up, cudaStream_t st) {
+  bounded_wait_probe_kernel<<<1, 32, 0, st>>>(limit, gave_up);
   GS_LAUNCHED();
   return GSFFT_OK;
 }

@@ -27,7 +27,7 @@ FLAG_FORCE_STREAM = 8
 FLAG_TC_BUCKET_FFT = 16
 FLAG_TC_RLFC_FFT = 32
 SELECTION_FLOOR = 1e-10
-OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE = range(7)
+OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE, ERR_TIMEOUT = range(8)
 
 NODE = np.dtype({"names": ["key", "x", "y"], "formats": ["<u4", "<f8", "<f8"],
                  "offsets": [0, 8, 16], "itemsize": 24})
@@ -116,6 +116,7 @@ def lib():
         "gsfft_stage_name": ([i], C.c_char_p),
         "gsfft_fft": ([P, P, ll, i, i, i, P], i),
         "gsfft_fft_tc": ([P, P, ll, i, i, P], i),
+        "gsfft_check_bounded_wait": ([ll, P], i),
         "gsfft_cutoff": ([P, i, i, i, i, P, P], i),
         "gsfft_cutoff_noalloc": ([P, i, i, i, i, P, P], i),
         "gsfft_cutoff_floor": ([P, i, i, i, i, d, P, P, P], i),

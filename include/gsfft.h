@@ -44,7 +44,10 @@ typedef enum {
   GSFFT_ERR_ALLOC = 3,       /* device or host allocation failed */
   GSFFT_ERR_CUDA = 4,        /* a CUDA runtime call failed (see gsfft_last_error) */
   GSFFT_ERR_UNSUPPORTED = 5, /* size or mode outside what the library supports */
-  GSFFT_ERR_STATE = 6        /* plan used before gsfft_plan_set_filter, or similar */
+  GSFFT_ERR_STATE = 6,       /* plan used before gsfft_plan_set_filter, or similar */
+  GSFFT_ERR_TIMEOUT = 7      /* a bounded device-side wait gave up (a copy or a
+                                tensor-core product never completed); the CUDA
+                                context stays usable */
 } gsfft_status;
 
 typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
@@ -368,6 +371,14 @@ int reverse_hash(int *d_J, int n, int B_thresh, int B, int a, int ai, int loop_t
 Node *estimate_values(int *d_I, int *I_F, complex_t *d_bins_f, int loops, int n,
                       int *permute, int B, complex_t *d_filter_freq, int loops_loc);
 int timesmod(const int x, const int a, const int n);
+
+/* Failure-detection self-check.  One CTA waits, with the bounded mbarrier
+ * wait every kernel of this library uses, on a barrier that nothing arrives
+ * on (no copy or product is issued against it) and gives up after
+ * limit_cycles SM clock cycles (1 .. 2^31).  Returns GSFFT_ERR_TIMEOUT, the
+ * status a run reports when one of its waits gives up; the CUDA context stays
+ * usable.  Synchronises stream. */
+int gsfft_check_bounded_wait(long long limit_cycles, void *stream);
 
 /* ---- misc -------------------------------------------------------------- */
 const char *gsfft_version(void);

@@ -80,3 +80,22 @@ def test_batch_graph_replays(G, torch_cuda):
     batch.close()
     for it in items:
         it[0].close()
+
+
+def test_bounded_wait_gives_up_and_context_survives(G, torch_cuda):
+    """Failure detection without a GPU fault: a wait on an mbarrier that
+    nothing arrives on (no copy or product in flight) gives up after its
+    limit, the library reports GSFFT_ERR_TIMEOUT -- the status a run returns
+    when one of its bounded waits gives up -- and the context keeps working
+    (a cutoff right after returns the right ids)."""
+    import numpy as np
+    torch = torch_cuda
+    L = G.lib()
+    assert L.gsfft_check_bounded_wait(20_000_000, None) == G.ERR_TIMEOUT  # about 10 ms
+    assert b"gave up" in L.gsfft_last_error()
+    assert L.gsfft_check_bounded_wait(0, None) == G.ERR_PARAM
+    s = np.arange(1000, dtype=np.float64)[::-1].copy()
+    d_s = torch.from_numpy(s).cuda()
+    d_o = torch.zeros(10, dtype=torch.int32, device="cuda")
+    G.cutoff(d_s.data_ptr(), 1000, 10, 1, 0, d_o.data_ptr())
+    np.testing.assert_array_equal(d_o.cpu().numpy(), np.arange(10))
