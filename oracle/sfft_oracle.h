@@ -14,8 +14,10 @@
  *
  * Parity is pinned by (a) the parameter KATs printed in the reference README
  * (README.md:84-90) and (b) golden vectors produced by the reference's own
- * stage functions (innerLoop.h:32-50, outerLoop.h:35-38) run on a GB300; see
- * tests/golden/.
+ * stage functions (innerLoop.h:32-50) and its outer_loop (outerLoop.cu:65-190),
+ * built from the reference's sources and run on a GB300 (oracle/build_ref.py,
+ * tests/golden/make_ref_fixtures.py); tests/test_ref_golden.py checks this
+ * restatement against them.
  */
 #ifndef SFFT_ORACLE_H_
 #define SFFT_ORACLE_H_
