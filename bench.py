@@ -593,11 +593,22 @@ def tune_batch(gsfft, torch, params, plans, filters, xs, drs, sh, timed, cache_p
         per_count[sc] = timed(lambda: b.launch(stream=sh), max(3, steps // 2))
         b.close()
     best = min(per_count, key=per_count.get)
+    # the same batch with every plan's voting in one persistent launch
+    persistent_ms = None
+    try:
+        b = gsfft.Batch(tuned, streams=best)
+        b.persistent_tail(True)
+        b.capture(ptrs, drs)
+        persistent_ms = timed(lambda: b.launch(stream=sh), max(3, steps // 2))
+        b.close()
+    except RuntimeError as e:
+        print(f"persistent tail unavailable: {e}", file=sys.stderr)
     forms = {}
     for t in shapes.values():
         f = "gather" if t.perm_filter_form == 2 else f"stream/{t.row_groups}"
         forms[f] = forms.get(f, 0) + 1
     details = {"groups": len(groups), "tune_s": round(tune_s, 1), "perm_filter_forms": forms,
+               "persistent_tail_ms_per_batch": round(persistent_ms, 4) if persistent_ms else None,
                "select_multi_launch_groups": sum(1 for t in shapes.values() if t.select_form == 2)}
     return tuned, best, per_count, details
 

@@ -28,6 +28,8 @@ struct Batch {
   cudaEvent_t fork = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  BatchTail *tail = nullptr;        // persistent tail of every plan (or none)
+  cudaEvent_t fork2 = nullptr;      // fork after the persistent tail
 };
 
 void batch_destroy(Batch *b) {
@@ -37,6 +39,8 @@ void batch_destroy(Batch *b) {
   for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
   for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->fork2) cudaEventDestroy(b->fork2);
+  batch_tail_free(b->tail);
   delete b;
 }
 
@@ -61,7 +65,8 @@ int batch_create(Plan *const *plans, int count, int nstreams, Batch **out) {
     b->streams.push_back(st);
     b->joins.push_back(ev);
   }
-  if (s == GSFFT_OK && cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+  if (s == GSFFT_OK && (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&b->fork2, cudaEventDisableTiming) != cudaSuccess))
     s = GSFFT_ERR_CUDA;
   if (s != GSFFT_OK) {
     batch_destroy(b);
@@ -79,17 +84,38 @@ int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, c
   for (int i = 0; i < S; i++) GS_CUDA(cudaStreamWaitEvent(b->streams[i], b->fork, 0));
   const int n = (int)b->plans.size();
   int s = GSFFT_OK;
+  auto join = [&]() {
+    // join every internal stream back into the caller's stream, also on error
+    for (int i = 0; i < S; i++) {
+      if (cudaEventRecord(b->joins[i], b->streams[i]) != cudaSuccess ||
+          cudaStreamWaitEvent(st, b->joins[i], 0) != cudaSuccess) {
+        set_last_error("gsfft_run_batched: join: %s", cudaGetErrorString(cudaGetLastError()));
+        if (s == GSFFT_OK) s = GSFFT_ERR_CUDA;
+      }
+    }
+  };
+  if (!b->tail) {
+    for (int i = 0; i < n && s == GSFFT_OK; i++)
+      s = plan_run(b->plans[i], d_x[i], offs + (size_t)i * MAX_RLFC_LOOPS, a + (size_t)i * MAX_LOOPS,
+                   ai + (size_t)i * MAX_LOOPS, b->streams[i % S], capturing);
+    join();
+    return s;
+  }
+  // fronts on the streams, every plan's voting in one persistent launch, then
+  // estimation and top-k on the streams
   for (int i = 0; i < n && s == GSFFT_OK; i++)
     s = plan_run(b->plans[i], d_x[i], offs + (size_t)i * MAX_RLFC_LOOPS, a + (size_t)i * MAX_LOOPS,
-                 ai + (size_t)i * MAX_LOOPS, b->streams[i % S], capturing);
-  // join every internal stream back into the caller's stream, also on error
-  for (int i = 0; i < S; i++) {
-    if (cudaEventRecord(b->joins[i], b->streams[i]) != cudaSuccess ||
-        cudaStreamWaitEvent(st, b->joins[i], 0) != cudaSuccess) {
-      set_last_error("gsfft_run_batched: join: %s", cudaGetErrorString(cudaGetLastError()));
-      if (s == GSFFT_OK) s = GSFFT_ERR_CUDA;
-    }
+                 ai + (size_t)i * MAX_LOOPS, b->streams[i % S], capturing, PH_FRONT);
+  join();
+  if (s == GSFFT_OK) s = batch_tail_launch(b->tail, st);
+  if (s == GSFFT_OK) {
+    GS_CUDA(cudaEventRecord(b->fork2, st));
+    for (int i = 0; i < S; i++) GS_CUDA(cudaStreamWaitEvent(b->streams[i], b->fork2, 0));
   }
+  for (int i = 0; i < n && s == GSFFT_OK; i++)
+    s = plan_run(b->plans[i], nullptr, nullptr, nullptr, nullptr, b->streams[i % S], capturing,
+                 PH_EST | PH_TOPK);
+  join();
   return s;
 }
 
@@ -133,6 +159,22 @@ int batch_capture(Batch *b, const void *const *d_x, const int *offs, const int *
   cudaGetLastError();  // a failed capture leaves its error behind
   cudaStreamDestroy(cs);
   return s;
+}
+
+int batch_set_persistent_tail(Batch *b, bool on) {
+  if (!b) return GSFFT_ERR_PARAM;
+  if (b->exec) {  // a captured graph holds the other form
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  batch_tail_free(b->tail);
+  b->tail = nullptr;
+  if (!on) return GSFFT_OK;
+  return batch_tail_create(b->plans.data(), (int)b->plans.size(), &b->tail);
 }
 
 int batch_launch(Batch *b, cudaStream_t st) {

@@ -282,6 +282,11 @@ int gsfft_batch_capture(gsfft_batch batch, const void *const *d_x, const int *h_
   return batch_capture(batch->impl, d_x, h_rlfc_offsets, h_a, h_ai);
 }
 
+int gsfft_batch_set_persistent_tail(gsfft_batch batch, int on) {
+  if (!batch) return GSFFT_ERR_PARAM;
+  return batch_set_persistent_tail(batch->impl, on != 0);
+}
+
 int gsfft_batch_launch(gsfft_batch batch, void *stream) {
   if (!batch) return GSFFT_ERR_PARAM;
   return batch_launch(batch->impl, S(stream));

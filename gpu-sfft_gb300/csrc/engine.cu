@@ -53,6 +53,11 @@ __global__ void run_begin_kernel(RunCtl *ctl, unsigned long long *rmax, int nrma
     bm[i] = 0u;
 }
 
+// the draws of a phased run, for the batch tail (batch_tail.cu)
+__global__ void store_draws_kernel(Draws d, Draws *out) {
+  if (threadIdx.x == 0) *out = d;
+}
+
 // hinv[idx] = conj(H)/|H|^2 with H = filter_freq[(n - d) mod n], d = idx - nb/2
 __global__ void hinv_kernel(const double2 *__restrict__ ff, int n, int nb, double2 *hinv) {
   const int idx = blockIdx.x * 256 + threadIdx.x;
@@ -138,6 +143,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   A(topk, sizeof(DevNode) * (size_t)p.k + 16);
   A(ctl, sizeof(RunCtl));
   A(d_epoch, sizeof(unsigned) * 4);
+  A(d_draws, sizeof(Draws));
   A(rmax, sizeof(unsigned long long) * (size_t)(p.RLFC_loops + p.loops));
   // perm+filter form: one ordered pass over x when that moves fewer DRAM bytes
   // than loops*w + RLFC_loops*W random reads (~80 bytes per random read)
@@ -228,7 +234,7 @@ void plan_destroy(Plan *P) {
   void *ptrs[] = {P->filt, P->hinv, P->rsamp, P->J2b, P->J2, P->bins, P->bsamp, P->J,
                   P->bm_j2, P->bm_sig, P->tile_tmp, P->vote, P->cand, P->cnt, P->blk,
                   P->nodes, P->mag2, P->topk_idx, P->topk, P->ctl, P->rmax, P->ybuf, P->bpart,
-                  P->filt_bm, P->d_epoch};
+                  P->filt_bm, P->d_epoch, P->d_draws};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
@@ -278,12 +284,16 @@ int plan_epoch_advance(Plan *P, cudaStream_t st) {
 }
 
 int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int *ai,
-             cudaStream_t st, bool capturing) {
+             cudaStream_t st, bool capturing, int phases) {
   if (!P->filter_set) return GSFFT_ERR_STATE;
+  if (phases < 1 || phases > PH_ALL) return GSFFT_ERR_PARAM;
   const gsfft_params &p = P->p;
   const int before = g_launch_counter;
   Draws d;
   memset(&d, 0, sizeof(d));
+  if (!(phases & PH_FRONT)) {
+    d = P->draws;  // the draws of the front phase queued last
+  } else {
   for (int r = 0; r < p.RLFC_loops; r++) {
     if (offs[r] < 0 || offs[r] >= p.n / p.W_RLFC) return GSFFT_ERR_PARAM;
     d.offs[r] = offs[r];
@@ -295,20 +305,27 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
     d.a[l] = a[l];
     d.ai[l] = ai[l];
   }
-  if (!capturing) GS_CHECK(plan_epoch_advance(P, st));
+  P->draws = d;
+  }
+  if (!capturing && (phases & PH_FRONT)) GS_CHECK(plan_epoch_advance(P, st));
   const int kb = P->precision == GSFFT_FP64 ? 8 : 4;
-  {
+  if (phases & PH_FRONT) {
     // about eight bitmap words per thread, at most 128 CTAs
     const long long bm_words = (long long)(p.W_RLFC / 32) * p.loops_loc;
     const int grid = (int)std::min<long long>(128, std::max<long long>(1, (bm_words + 2047) / 2048));
     run_begin_kernel<<<grid, 256, 0, st>>>(P->ctl, (unsigned long long *)P->rmax, p.RLFC_loops + p.loops,
                                            P->d_epoch, P->bm_sig, bm_words);
+    GS_LAUNCHED();
+    if (phases != PH_ALL) {
+      // a phased run (batch tail): the tail reads this run's draws from the device
+      store_draws_kernel<<<1, 32, 0, st>>>(d, P->d_draws);
+      GS_LAUNCHED();
+    }
   }
-  GS_LAUNCHED();
   void *rmax_w = P->rmax;  // RLFC rows, then bucket rows (u64 in FP64, u32 in FP32)
   void *rmax_b = (char *)P->rmax + (size_t)kb * p.RLFC_loops;
   cudaEvent_t *ev = nullptr;
-  if (P->timing && !capturing && P->timed_runs < 512) {
+  if (P->timing && !capturing && phases == PH_ALL && P->timed_runs < 512) {
     const size_t need = (size_t)(P->timed_runs + 1) * (2 * ST_COUNT);
     while (P->events.size() < need) {
       cudaEvent_t e;
@@ -328,6 +345,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   if (ev) GS_CUDA(cudaEventRecord(ev[2 * (s) + 1], q))
   const bool quirk = (P->flags & GSFFT_FLAG_QUIRK_RESIDUE) != 0;
 
+  if (phases & PH_FRONT) {
   // A5 (+ RLFC sub-sampling when streaming): bins of every loop
   BEGIN(ST_PERM_FILTER);
   if (P->use_stream)
@@ -400,8 +418,12 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
                                     P->bm_sig, P->ctl, st));
   END(ST_J2);
 
-  // A7: voting, one location loop after the other (after the side stream)
+  // the side stream joins back before the voting
   GS_CUDA(cudaStreamWaitEvent(st, P->ev_join, 0));
+  }  // front
+
+  if (phases & PH_VOTE) {
+  // A7: voting, one location loop after the other
   BEGIN(ST_VOTE);
   const size_t wW = (size_t)p.W_RLFC / 32;
   for (int l = 0; l < p.loops_loc; l++)
@@ -409,6 +431,9 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
                               P->bm_sig + wW * l, d, p.loops_thresh, P->d_epoch, P->vote, P->cand,
                               P->cap, P->cnt, P->blk, P->ctl, l + 1 >= p.loops_thresh, st));
   END(ST_VOTE);
+  }  // voting
+
+  if (phases & PH_EST) {
   // A8: estimation; A9: k largest
   BEGIN(ST_ESTIMATE);
   // the grid covers 8k candidates at one per thread (about 4.8k at the
@@ -417,17 +442,21 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
                            (int)std::min<long long>(P->cap, 8LL * p.k), P->bins, p.loops, p.n, p.B, d,
                            P->hinv, P->nodes, P->mag2, st));
   END(ST_ESTIMATE);
+  }  // estimation
+
+  if (phases & PH_TOPK) {
   BEGIN(ST_TOPK);
   GS_CHECK(select_top(P->mag2, 8, P->cap, &P->ctl->cand_count, p.k, 1, P->cap, P->topk_idx, p.k,
                       &P->ctl->n_topk, P->selK, st));
   GS_CHECK(launch_gather_nodes(P->nodes, P->topk_idx, &P->ctl->n_topk, p.k, P->topk, st));
   END(ST_TOPK);
+  }  // top-k
 #undef BEGIN
 #undef END
 #undef BEGIN_ON
 #undef END_ON
-  P->launches_per_run = g_launch_counter - before;
-  P->ran = true;
+  if (phases == PH_ALL) P->launches_per_run = g_launch_counter - before;
+  if (phases & PH_TOPK) P->ran = true;
   return GSFFT_OK;
 }
 

@@ -48,6 +48,8 @@ struct Plan {
   bool tc_rlfc = false;    // RLFC FFT with a tensor-core first pass
   double floor_rel = 1e-10;
   gsfft_plan_tuning tuning = {};  // the stage shapes in use (rules' choices filled in)
+  Draws draws = {};               // the draws of the last front phase queued
+  Draws *d_draws = nullptr;       // device copy of them (phased runs)
   // optional per-stage CUDA-event timing (one event set per run, up to 512 runs)
   // side stream of the bucket FFT and cutoff (they need only the perm+filter)
   cudaStream_t side = nullptr;
@@ -65,8 +67,13 @@ int plan_set_filter(Plan *P, const void *d_filter_time, const void *d_filter_fre
                     cudaStream_t st);
 // capturing = true while a CUDA graph records the run: the host-side epoch
 // bookkeeping and stage timing are then left to whoever launches the graph.
+// phases: which part of the run to queue -- PH_FRONT (run state, perm+filter,
+// FFTs, cutoffs, residue bitmaps; takes the draws), PH_VOTE (voting), PH_EST
+// (estimation), PH_TOPK (the k largest) -- so that a batch can run the voting
+// of all its plans in one persistent launch between the fronts and the rest.
+enum { PH_FRONT = 1, PH_VOTE = 2, PH_TOPK = 4, PH_EST = 8, PH_ALL = 15 };
 int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int *ai,
-             cudaStream_t st, bool capturing = false);
+             cudaStream_t st, bool capturing = false, int phases = PH_ALL);
 // host side of a run's epoch step (clears the vote table when the 24-bit
 // epoch would wrap); called once per queued run, before the run's kernels
 int plan_epoch_advance(Plan *P, cudaStream_t st);
@@ -80,6 +87,13 @@ int plan_debug(Plan *P, int *h_J2, int *num_RLFC, int *h_J, void *h_bins, cudaSt
 int launch_hinv(const double2 *d_ff, int n, int nb, double2 *hinv, cudaStream_t st);
 int launch_convert_taps(const double2 *d_ft, void *dst, int w, bool to_float, cudaStream_t st);
 
+// persistent tail of a batch (batch_tail.cu): the voting of every plan in
+// one cooperative launch
+struct BatchTail;
+int batch_tail_create(Plan *const *plans, int count, BatchTail **out);
+int batch_tail_launch(BatchTail *t, cudaStream_t st);
+void batch_tail_free(BatchTail *t);
+
 // batched runs over several plans (batch.cu)
 struct Batch;
 int batch_create(Plan *const *plans, int count, int nstreams, Batch **out);
@@ -88,6 +102,7 @@ int batch_run(Batch *b, const void *const *d_x, const int *offs, const int *a, c
 int batch_capture(Batch *b, const void *const *d_x, const int *offs, const int *a, const int *ai);
 int batch_launch(Batch *b, cudaStream_t st);
 void batch_destroy(Batch *b);
+int batch_set_persistent_tail(Batch *b, bool on);
 
 // signal ingest and device-side evaluation (host_io.cu)
 int launch_to_float(const complex_t *in, void *out, long long n, cudaStream_t st);

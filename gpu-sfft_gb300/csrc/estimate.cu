@@ -12,7 +12,7 @@
 // in FP64 per loop (bins are promoted from FP32 in the mixed path).  The
 // median of the real parts and of the imaginary parts is taken separately,
 // element (loops-1)/2 of the ascending order (:855-861).
-#include "stages.cuh"
+#include "estimate_dev.cuh"
 
 namespace gsfft {
 
@@ -20,84 +20,14 @@ namespace {
 
 constexpr int ET = 128;
 
-// Order-preserving integer key of a double (finite values): comparing keys
-// as unsigned integers orders the values, so the ranking below runs on the
-// integer pipe instead of GB300's narrow FP64 pipe.  (-0.0 ranks just below
-// +0.0; both are the same value.)
-__device__ __forceinline__ unsigned long long dkey(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
-}
-
-// Element (L-1)/2 of the ascending order (ties by index), by rank counting.
-__device__ __forceinline__ double median_of(const double *v, int L) {
-  const int want = (L - 1) / 2;
-  double res = v[0];
-  for (int i = 0; i < L; i++) {
-    const unsigned long long ki = dkey(v[i]);
-    int rank = 0;
-    for (int j = 0; j < L; j++) {
-      const unsigned long long kj = dkey(v[j]);
-      rank += (kj < ki) || (kj == ki && j < i);
-    }
-    if (rank == want) res = v[i];
-  }
-  return res;
-}
-
-// Compile-time loop count: the per-loop values and keys live in registers.
-template <int L>
-__device__ __forceinline__ double median_reg(const double (&v)[L]) {
-  constexpr int want = (L - 1) / 2;
-  unsigned long long k[L];
-#pragma unroll
-  for (int i = 0; i < L; i++) k[i] = dkey(v[i]);
-  double res = v[0];
-#pragma unroll
-  for (int i = 0; i < L; i++) {
-    int rank = 0;
-#pragma unroll
-    for (int j = 0; j < L; j++) rank += (k[j] < k[i]) || (k[j] == k[i] && j < i);
-    if (rank == want) res = v[i];
-  }
-  return res;
-}
-
 template <typename T, int L>
 __global__ void __launch_bounds__(ET)
 estimate_kernel_fixed(const int *__restrict__ cand, const RunCtl *ctl, int cap,
                       const typename Cx<T>::V *__restrict__ bins, unsigned nmask, int lognb, int B,
                       Draws d, const double2 *__restrict__ hinv, DevNode *nodes, double *mag2) {
   pdl_enter();
-  const int count = min(ctl->cand_count, cap);
-  const int nb = 1 << lognb;
-  for (int i = blockIdx.x * ET + threadIdx.x; i < count; i += gridDim.x * ET) {
-    const unsigned loc = (unsigned)cand[i];
-    double vr[L], vi[L];
-#pragma unroll
-    for (int j = 0; j < L; j++) {
-      const unsigned p = ((unsigned)d.ai[j] * loc) & nmask;
-      int h = (int)(p >> lognb);
-      int dd = (int)(p & (unsigned)(nb - 1));
-      if (dd > nb / 2) {
-        h = (h + 1) & (B - 1);
-        dd -= nb;
-      }
-      const double2 H = __ldg(&hinv[dd + nb / 2]);
-      const typename Cx<T>::V bv = bins[(size_t)j * B + h];
-      const double bx = (double)bv.x, by = (double)bv.y;
-      vr[j] = fma(bx, H.x, -(by * H.y));
-      vi[j] = fma(bx, H.y, by * H.x);
-    }
-    const double re = median_reg<L>(vr), im = median_reg<L>(vi);
-    DevNode nd;
-    nd.key = loc;
-    nd.pad = 0;
-    nd.x = re;
-    nd.y = im;
-    nodes[i] = nd;
-    mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
-  }
+  estimate_block<T, L>(cand, ctl, cap, bins, nmask, lognb, B, d, hinv, nodes, mag2, (int)blockIdx.x,
+                       (int)gridDim.x);
 }
 
 template <typename T>

@@ -1,0 +1,97 @@
+// Device code of the estimation stage (A8), shared by the per-plan kernels
+// (estimate.cu) and the persistent batch-tail kernel (batch_tail.cu).  The
+// candidate list and count may have been written by another block of the
+// same launch, so they are read past L1 (ld.global.cg).
+#pragma once
+#include "stages.cuh"
+
+namespace gsfft {
+
+namespace {
+
+// Order-preserving integer key of a double (finite values): comparing keys
+// as unsigned integers orders the values, so the ranking below runs on the
+// integer pipe instead of GB300's narrow FP64 pipe.  (-0.0 ranks just below
+// +0.0; both are the same value.)
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Element (L-1)/2 of the ascending order (ties by index), by rank counting.
+__device__ __forceinline__ double median_of(const double *v, int L) {
+  const int want = (L - 1) / 2;
+  double res = v[0];
+  for (int i = 0; i < L; i++) {
+    const unsigned long long ki = dkey(v[i]);
+    int rank = 0;
+    for (int j = 0; j < L; j++) {
+      const unsigned long long kj = dkey(v[j]);
+      rank += (kj < ki) || (kj == ki && j < i);
+    }
+    if (rank == want) res = v[i];
+  }
+  return res;
+}
+
+// Compile-time loop count: the per-loop values and keys live in registers.
+template <int L>
+__device__ __forceinline__ double median_reg(const double (&v)[L]) {
+  constexpr int want = (L - 1) / 2;
+  unsigned long long k[L];
+#pragma unroll
+  for (int i = 0; i < L; i++) k[i] = dkey(v[i]);
+  double res = v[0];
+#pragma unroll
+  for (int i = 0; i < L; i++) {
+    int rank = 0;
+#pragma unroll
+    for (int j = 0; j < L; j++) rank += (k[j] < k[i]) || (k[j] == k[i] && j < i);
+    if (rank == want) res = v[i];
+  }
+  return res;
+}
+
+// Estimates of candidates bid * blockDim.x + threadIdx.x, then every
+// nblk * blockDim.x further (a grid-stride loop over nblk blocks).
+template <typename T, int L>
+__device__ __forceinline__ void estimate_block(const int *__restrict__ cand, const RunCtl *ctl,
+                                               int cap, const typename Cx<T>::V *__restrict__ bins,
+                                               unsigned nmask, int lognb, int B, const Draws &d,
+                                               const double2 *__restrict__ hinv, DevNode *nodes,
+                                               double *mag2, int bid, int nblk) {
+  const int count = min(__ldcg(&ctl->cand_count), cap);
+  const int nb = 1 << lognb;
+  const int nt = (int)blockDim.x;
+  for (int i = bid * nt + threadIdx.x; i < count; i += nblk * nt) {
+    const unsigned loc = (unsigned)__ldcg(&cand[i]);
+    double vr[L], vi[L];
+#pragma unroll
+    for (int j = 0; j < L; j++) {
+      const unsigned p = ((unsigned)d.ai[j] * loc) & nmask;
+      int h = (int)(p >> lognb);
+      int dd = (int)(p & (unsigned)(nb - 1));
+      if (dd > nb / 2) {
+        h = (h + 1) & (B - 1);
+        dd -= nb;
+      }
+      const double2 H = __ldg(&hinv[dd + nb / 2]);
+      const typename Cx<T>::V bv = bins[(size_t)j * B + h];
+      const double bx = (double)bv.x, by = (double)bv.y;
+      vr[j] = fma(bx, H.x, -(by * H.y));
+      vi[j] = fma(bx, H.y, by * H.x);
+    }
+    const double re = median_reg<L>(vr), im = median_reg<L>(vi);
+    DevNode nd;
+    nd.key = loc;
+    nd.pad = 0;
+    nd.x = re;
+    nd.y = im;
+    nodes[i] = nd;
+    mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+  }
+}
+
+}  // namespace
+
+}  // namespace gsfft

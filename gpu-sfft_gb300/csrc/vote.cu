@@ -29,46 +29,11 @@
 //    bucket's first STASH candidates in window order, so the write pass
 //    copies them instead of walking the window and the vote table again
 //    (buckets with more candidates are walked again).
-#include "stages.cuh"
+#include "vote_dev.cuh"
 
 namespace gsfft {
 
 namespace {
-
-constexpr int VT = 256;  // threads per block in this file
-
-__device__ __forceinline__ unsigned blk_excl_scan(unsigned v, unsigned *ws, unsigned *total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) ws[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    unsigned w = lane < VT / 32 ? ws[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    if (lane < VT / 32) ws[lane] = w;
-  }
-  __syncthreads();
-  unsigned base = wid ? ws[wid - 1] : 0;
-  unsigned tot = ws[VT / 32 - 1];
-  __syncthreads();
-  if (total) *total = tot;
-  return base + x - v;
-}
-
-__device__ __forceinline__ unsigned blk_sum(unsigned v, unsigned *ws) {
-  unsigned t;
-  blk_excl_scan(v, ws, &t);
-  return t;
-}
 
 // ------------------------------------------------------------ J2 merge
 constexpr int WORDS_PER_THREAD = 8;
@@ -160,223 +125,18 @@ __global__ void sigma_from_blocks_kernel(const int *__restrict__ J2b, int total,
   }
 }
 
-// ------------------------------------------------------------ voting
-struct WalkArgs {
-  const int *J;
-  int Bt, n, nb, W;
-  const unsigned *bm;
-  const int *fmax;
-  unsigned a;
-};
-
-// low = ceil((J - 0.5) * n/B) reduced mod n (innerLoop.cu:792), in integers.
-__device__ __forceinline__ int window_low(int J, int n, int nb) {
-  const long long v = (2LL * J - 1) * nb;  // 2 * (J - 0.5) * nb
-  const long long c = v >= 0 ? (v + 1) / 2 : -((-v) / 2);
-  return (int)((c + n) & (long long)(n - 1));
-}
-
-// One warp per heavy bucket.  The window [low, low + n/B) is cut into chunks;
-// in chunk c lane L holds a 32-bit mask of visited positions (window offsets
-// 1024c + 32L .. +31 when the window is 32-aligned, else the single offset
-// 32c + L).  Chunks, lanes and bits in ascending order give the window in
-// ascending order.  chunk_fn(mask, pos_of_bit) is called once per chunk by
-// every lane (warp-uniform trip count).
-struct ChunkPos {
-  int r0, base, key, W, n, aligned;
-  // position of bit t of this lane's mask
-  __device__ __forceinline__ int operator()(int t) const {
-    const int rr = aligned ? r0 + t : r0;
-    const int blk = (rr >= key) ? base : ((base + W) & (n - 1));
-    return blk + rr;
-  }
-};
-
-template <class F>
-__device__ __forceinline__ void for_each_chunk(const WalkArgs &w, int J, F &&chunk_fn) {
-  const int lane = threadIdx.x & 31;
-  const int low = window_low(J, w.n, w.nb);
-  const int key = low & (w.W - 1);
-  if (key > *w.fmax) return;  // reference clamp: nothing visited
-  const int base = low - key;
-  const int aligned = ((key & 31) == 0 && (w.nb & 31) == 0) ? 1 : 0;
-  const int span = aligned ? 1024 : 32;
-  for (int c0 = 0; c0 < w.nb; c0 += span) {
-    unsigned mask = 0;
-    int r0 = 0;
-    if (aligned) {
-      const int off = c0 + lane * 32;
-      if (off < w.nb) {
-        r0 = key + off;
-        if (r0 >= w.W) r0 -= w.W;  // aligned words never straddle W
-        mask = __ldg(&w.bm[r0 >> 5]);
-      }
-    } else {
-      const int off = c0 + lane;
-      if (off < w.nb) {
-        int r = key + off;
-        if (r >= w.W) r -= w.W;
-        r0 = r;
-        mask = (__ldg(&w.bm[r >> 5]) >> (r & 31)) & 1u;
-      }
-    }
-    ChunkPos pos{r0, base, key, w.W, w.n, aligned};
-    chunk_fn(mask, pos);
-  }
-}
-
-__device__ __forceinline__ unsigned warp_excl_scan(unsigned v, unsigned *total) {
-  const int lane = threadIdx.x & 31;
-  unsigned x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  *total = __shfl_sync(0xffffffffu, x, 31);
-  return x - v;
-}
-
-constexpr int WPB = VT / 32;  // buckets (warps) per block
-constexpr int STASH = 32;     // candidates recorded per heavy bucket by the count pass
-
 __global__ void __launch_bounds__(VT)
 vote_count_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, unsigned *vote, int *cnt,
                   int *blk, int *blk_pre, int *stash, RunCtl *ctl) {
   pdl_enter();
-  const unsigned epoch = *epoch_p;
-  __shared__ unsigned ws[VT / 32];
-  __shared__ int is_last;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t = blockIdx.x * WPB + warp;
-  unsigned c = 0;
-  if (t < w.Bt) {
-    const unsigned nmask = (unsigned)w.n - 1u;
-    int *const slot = stash + (size_t)t * STASH;
-    unsigned recorded = 0;  // this bucket's candidates so far (warp-uniform)
-    for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
-      // up to four visited positions at a time: their table reads are
-      // independent, so they overlap instead of paying one DRAM latency each
-      unsigned app = 0;  // bits of this lane's mask whose count reached the threshold
-      while (mask) {
-        unsigned loc[4], e[4];
-        int nq = 0;
-        const unsigned before = mask;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (mask) {
-            const int bq = __ffs(mask) - 1;
-            mask &= mask - 1;
-            loc[q] = ((unsigned)pos(bq) * w.a) & nmask;
-            nq = q + 1;
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-          if (q < nq) e[q] = vote[loc[q]];
-        unsigned hitq = 0;  // bit q: position q of this round reached the threshold
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (q < nq) {
-            const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
-            vote[loc[q]] = (epoch << 8) | cv;
-            hitq |= (unsigned)(cv == thresh) << q;
-          }
-        }
-        // the round's positions are the lowest set bits of `before`, in order
-        unsigned taken = before & ~mask;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const unsigned low = taken & (0u - taken);
-          taken ^= low;
-          if ((hitq >> q) & 1u) app |= low;
-        }
-      }
-      c += (unsigned)__popc(app);
-      // window order: chunks, then lanes, then bits (as the write pass walks)
-      if (__any_sync(0xffffffffu, app != 0u)) {
-        unsigned ctot;
-        unsigned o = recorded + warp_excl_scan((unsigned)__popc(app), &ctot);
-        while (app) {
-          const int b = __ffs(app) - 1;
-          app &= app - 1;
-          if (o < (unsigned)STASH) slot[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
-          o++;
-        }
-        recorded += ctot;
-      }
-    });
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-  if (lane == 0 && t < w.Bt) cnt[t] = (int)c;
-  const unsigned s = blk_sum(lane == 0 ? c : 0u, ws);
-  // last block: exclusive scan of the block counts.  Only the block count has
-  // to be visible to it, so only thread 0 fences (a fence in every thread
-  // would wait for that thread's vote-table writes to reach memory).
-  if (threadIdx.x == 0) {
-    blk[blockIdx.x] = (int)s;
-    __threadfence();
-    const unsigned tk = atomicAdd(&ctl->ticket, 1u);
-    is_last = tk == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  // Each thread scans a contiguous run of block counts: all its L2 loads are
-  // independent, then one block scan (the serial tail used to pay an L2 round
-  // trip and three barriers per 256 counts).
-  const int nblk = (int)gridDim.x;
-  const int per = (nblk + VT - 1) / VT;
-  const int i0 = min(nblk, (int)threadIdx.x * per), i1 = min(nblk, i0 + per);
-  unsigned sum = 0;
-  for (int i = i0; i < i1; i++) sum += (unsigned)__ldcg(&blk[i]);
-  unsigned tot;
-  unsigned run = blk_excl_scan(sum, ws, &tot);
-  for (int i = i0; i < i1; i++) {
-    blk_pre[i] = (int)run;
-    run += (unsigned)__ldcg(&blk[i]);
-  }
-  if (threadIdx.x == 0) {
-    blk_pre[nblk] = (int)tot;
-    ctl->ticket = 0;
-  }
+  vote_count_block(w, *epoch_p, thresh, vote, cnt, blk, blk_pre, stash, ctl, (int)blockIdx.x,
+                   (int)gridDim.x);
 }
 
-// Location loops before the (loops_thresh-1)-th cannot bring any count to
-// the threshold: they only record their votes.
 __global__ void __launch_bounds__(VT)
 vote_mark_kernel(WalkArgs w, const unsigned *epoch_p, unsigned *vote) {
   pdl_enter();
-  const unsigned epoch = *epoch_p;
-  const int warp = threadIdx.x >> 5;
-  const int t = blockIdx.x * WPB + warp;
-  if (t >= w.Bt) return;
-  const unsigned nmask = (unsigned)w.n - 1u;
-  for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
-    while (mask) {
-      unsigned loc[4], e[4];
-      int nq = 0;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        if (mask) {
-          const int b = __ffs(mask) - 1;
-          mask &= mask - 1;
-          loc[q] = ((unsigned)pos(b) * w.a) & nmask;
-          nq = q + 1;
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (q < nq) e[q] = vote[loc[q]];
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (q < nq) {
-          const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
-          vote[loc[q]] = (epoch << 8) | cv;
-        }
-    }
-  });
+  vote_mark_block(w, *epoch_p, vote, (int)blockIdx.x);
 }
 
 __global__ void __launch_bounds__(VT)
@@ -384,73 +144,8 @@ vote_write_kernel(WalkArgs w, const unsigned *epoch_p, unsigned thresh, const un
                   const int *__restrict__ cnt, const int *__restrict__ blk_pre, int nblk,
                   const int *__restrict__ stash, int *cand, int cap, RunCtl *ctl) {
   pdl_enter();
-  __shared__ unsigned ws[VT / 32];
-  __shared__ int is_last;
-  const int base_prev = ctl->cand_count;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t = blockIdx.x * WPB + warp;
-  const unsigned c = (t < w.Bt && lane == 0) ? (unsigned)cnt[t] : 0u;
-  unsigned tot;
-  const unsigned wpre = blk_excl_scan(c, ws, &tot);  // lane 0 of each warp carries its count
-  long long next = (long long)base_prev + blk_pre[blockIdx.x] + __shfl_sync(0xffffffffu, wpre, 0);
-  const unsigned cw = __shfl_sync(0xffffffffu, c, 0);
-  if (cw && cw <= (unsigned)STASH) {
-    // recorded by the count pass in window order
-    const int *slot = stash + (size_t)t * STASH;
-    for (unsigned j = lane; j < cw; j += 32) {
-      const long long o = next + j;
-      if (o < cap) cand[o] = slot[j];
-    }
-  } else if (cw) {
-    const unsigned nmask = (unsigned)w.n - 1u;
-    const unsigned want = (*epoch_p << 8) | thresh;
-    for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
-      // appended positions of this lane, in bit order
-      unsigned app = 0;
-      unsigned m = mask;
-      while (m) {
-        unsigned loc[4], bit[4];
-        int nq = 0;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (m) {
-            bit[q] = __ffs(m) - 1;
-            m &= m - 1;
-            loc[q] = ((unsigned)pos((int)bit[q]) * w.a) & nmask;
-            nq = q + 1;
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-          if (q < nq && vote[loc[q]] == want) app |= 1u << bit[q];
-      }
-      unsigned ctot;
-      long long o = next + warp_excl_scan((unsigned)__popc(app), &ctot);
-      while (app) {
-        const int b = __ffs(app) - 1;
-        app &= app - 1;
-        if (o < cap) cand[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
-        o++;
-      }
-      next += ctot;
-    });
-  }
-  // the last block to finish publishes the new candidate count; every block
-  // read the old one before its thread 0 takes a ticket (barrier + fence)
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned tk = atomicAdd(&ctl->ticket, 1u);
-    is_last = tk == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (is_last && threadIdx.x == 0) {
-    __threadfence();
-    const long long nc = (long long)base_prev + blk_pre[nblk];
-    ctl->cand_count = (int)(nc > 0x7fffffffLL ? 0x7fffffffLL : nc);
-    if (nc > cap) ctl->overflow = 1;
-    ctl->ticket = 0;
-  }
+  vote_write_block(w, *epoch_p, thresh, vote, cnt, blk_pre, stash, cand, cap, ctl, (int)blockIdx.x,
+                   nblk);
 }
 
 }  // namespace

@@ -103,6 +103,7 @@ def lib():
         "gsfft_run_batched": ([P, C.POINTER(P), P, P, P, P], i),
         "gsfft_batch_capture": ([P, C.POINTER(P), P, P, P], i),
         "gsfft_batch_launch": ([P, P], i),
+        "gsfft_batch_set_persistent_tail": ([P, i], i),
         "gsfft_tc_dft64": ([P, P, i, P], i),
         "gsfft_alloc": ([C.POINTER(P), C.c_size_t], i),
         "gsfft_free": ([P], i),
@@ -238,6 +239,12 @@ class Batch:
 
     def launch(self, stream=0):
         check(lib().gsfft_batch_launch(self.h, stream or None), "gsfft_batch_launch")
+
+    def persistent_tail(self, on=True):
+        """Voting of every plan in one persistent launch
+        (gsfft_batch_set_persistent_tail); drops a captured graph."""
+        check(lib().gsfft_batch_set_persistent_tail(self.h, int(on)),
+              "gsfft_batch_set_persistent_tail")
 
     def close(self):
         if self.h:

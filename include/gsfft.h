@@ -227,6 +227,17 @@ int gsfft_batch_capture(gsfft_batch batch, const void *const *d_x, const int *h_
                         const int *h_a, const int *h_ai);
 int gsfft_batch_launch(gsfft_batch batch, void *stream);
 
+/* Persistent voting: on != 0 makes the batch's runs (gsfft_run_batched, and
+ * graphs captured afterwards) queue every plan's front -- run state,
+ * perm+filter, FFTs, cutoffs, residue bitmaps -- on its stream, then the
+ * reverse-hash voting of all plans in ONE cooperative persistent launch (its
+ * blocks take runs of the plans' vote blocks from a device work queue in
+ * stage order, with bounded waits that end in GSFFT_ERR_TIMEOUT), then every
+ * plan's estimation and top-k on its stream.  Results equal the plans' single
+ * runs.  Plans with at most 16 location loops (GSFFT_ERR_UNSUPPORTED
+ * otherwise).  Drops a captured graph; on = 0 returns to per-plan voting. */
+int gsfft_batch_set_persistent_tail(gsfft_batch batch, int on);
+
 /* ---- host I/O and evaluation ---------------------------------------- */
 
 /* Device memory and copies for callers that do not link the CUDA runtime

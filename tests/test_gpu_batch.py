@@ -1,5 +1,7 @@
 """gsfft_run_batched: a batch of plans with different sizes, parameters and
-precisions gives exactly the results of running each plan alone."""
+precisions gives exactly the results of running each plan alone -- with
+per-plan tails and with the persistent tail (every plan's voting and
+estimation in one launch)."""
 import numpy as np
 import pytest
 
@@ -31,8 +33,9 @@ def _setup(G, torch, cfg, prec, seed):
     return plan, d_x, draws, (d_ft, d_ff)
 
 
+@pytest.mark.parametrize("persistent", [False, True])
 @pytest.mark.parametrize("streams", [1, 4])
-def test_batched_equals_single(G, torch_cuda, streams):
+def test_batched_equals_single(G, torch_cuda, streams, persistent):
     torch = torch_cuda
     items = [_setup(G, torch, cfg, prec, 100 + i) for i, (cfg, prec) in enumerate(CASES)]
     single = []
@@ -40,6 +43,8 @@ def test_batched_equals_single(G, torch_cuda, streams):
         plan.run(d_x.data_ptr(), *draws)
         single.append(plan.results())
     batch = G.Batch([it[0] for it in items], streams=streams)
+    if persistent:
+        batch.persistent_tail(True)
     batch.run([it[1].data_ptr() for it in items], [it[2] for it in items])
     torch.cuda.synchronize()
     for (plan, _, _, _), ref in zip(items, single):
@@ -52,13 +57,16 @@ def test_batched_equals_single(G, torch_cuda, streams):
         it[0].close()
 
 
-def test_batch_graph_replays(G, torch_cuda):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_batch_graph_replays(G, torch_cuda, persistent):
     """A captured batch replays with one graph launch: on new signal contents
     written into the captured buffers, and twice in a row (each replay must
     count votes afresh), it gives exactly the single-plan results."""
     torch = torch_cuda
     items = [_setup(G, torch, cfg, prec, 200 + i) for i, (cfg, prec) in enumerate(CASES)]
     batch = G.Batch([it[0] for it in items], streams=4)
+    if persistent:
+        batch.persistent_tail(True)
     batch.capture([it[1].data_ptr() for it in items], [it[2] for it in items])
     stream = torch.cuda.Stream()
     for rep in range(2):
