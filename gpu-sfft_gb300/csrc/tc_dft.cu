@@ -187,76 +187,135 @@ tc_dft64_kernel(const float2 *__restrict__ x, float2 *__restrict__ y, int nvec, 
 
 // The three bf16 parts of F' (the real form of DFT_64 with the real and
 // imaginary rows of each output interleaved: row 2o = Re, row 2o + 1 = Im of
-// output o) in the K-major layout, 3 x 32 KiB, built once per FFT plan.
+// output o), built once per FFT plan in the tensor-memory layout of an A
+// operand: part p, row m (a TMEM lane), 32-bit column c holding k = 2c in its
+// low and k = 2c + 1 in its high half.  In global memory a part is 128 rows of
+// 256 bytes whose 16-byte chunks are XOR-swizzled by the row (chunk ch of row
+// m at (ch ^ (m & 15)) * 16), so that a warp reading chunk ch of 32 rows from
+// a shared-memory copy touches every bank once per 128 bytes.
 // With theta = 2 pi o i / 64 and W = e^{-i theta}:
 //   Re(W x) = cos(theta) xr + sin(theta) xi,  Im(W x) = cos(theta) xi - sin(theta) xr.
+constexpr int FT_ROW_BYTES = 256;                   // 64 columns x 4 bytes
+constexpr int FT_PART_BYTES = TC_M * FT_ROW_BYTES;  // 32 KiB
 __global__ void tc_build_F_kernel(unsigned char *F) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= TC_M * TC_K) return;
-  const int m = e / TC_K, k = e % TC_K;
-  const int o = m >> 1, i = k & 63;
-  double s, c;
-  sincospi(2.0 * (double)((o * i) & 63) / 64.0, &s, &c);
-  float f;
-  if ((m & 1) == 0) f = (k < 64) ? (float)c : (float)s;
-  else f = (k < 64) ? (float)(-s) : (float)c;
-  __nv_bfloat16 p0, p1, p2;
-  split3(f, p0, p1, p2);
-  const int off = kmajor_off(m, k, TC_K);
-  *reinterpret_cast<__nv_bfloat16 *>(F + off) = p0;
-  *reinterpret_cast<__nv_bfloat16 *>(F + A_BYTES + off) = p1;
-  *reinterpret_cast<__nv_bfloat16 *>(F + 2 * A_BYTES + off) = p2;
+  if (e >= TC_M * (TC_K / 2)) return;
+  const int m = e / (TC_K / 2), col = e % (TC_K / 2);
+  const int o = m >> 1;
+  unsigned w[3] = {0u, 0u, 0u};
+  for (int h = 0; h < 2; h++) {
+    const int k = 2 * col + h, i = k & 63;
+    double sn, cs;
+    sincospi(2.0 * (double)((o * i) & 63) / 64.0, &sn, &cs);
+    float f;
+    if ((m & 1) == 0) f = (k < 64) ? (float)cs : (float)sn;
+    else f = (k < 64) ? (float)(-sn) : (float)cs;
+    __nv_bfloat16 p[3];
+    split3(f, p[0], p[1], p[2]);
+    for (int pp = 0; pp < 3; pp++) w[pp] |= (unsigned)__bfloat16_as_ushort(p[pp]) << (16 * h);
+  }
+  const int ch = col >> 2;
+  const int off = m * FT_ROW_BYTES + ((ch ^ (m & 15)) << 4) + (col & 3) * 4;
+  for (int pp = 0; pp < 3; pp++) *reinterpret_cast<unsigned *>(F + pp * FT_PART_BYTES + off) = w[pp];
 }
 
 // ---- radix-4096 pass ------------------------------------------------------
-constexpr int TP_THREADS = 256;  // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31
-constexpr int TP_N = 128;        // vectors per product: two sub-transforms x 64
-constexpr int X_BYTES = TP_N * TC_K * 2;  // one bf16 part of the X operand: 32 KiB
-constexpr int TW_BYTES = 4096 * 8;        // exp(-2 pi i m / 4096), m < 4096
-constexpr int TC4K_SMEM = 3 * A_BYTES + 3 * X_BYTES + TW_BYTES + 64;
-static_assert(TC4K_SMEM <= 227 * 1024, "radix-4096 pass exceeds the shared memory of a CTA");
+constexpr int TP_N = 128;                 // vectors per product: two sub-transforms x 64
+constexpr int X_BYTES = TP_N * TC_K * 2;  // one bf16 part of an operand: 32 KiB
+constexpr int TQ_XBUF = 3 * X_BYTES;      // one operand buffer (three parts): 96 KiB
+constexpr int TQ_TW_BYTES = 64 * 64 * 8;  // W4096^(r1 k2) at [r1][k2]
+constexpr int TQ_LD_WARPS = 8;            // loaders: global -> bf16 parts of product 1's operand
+constexpr int TQ_EP_WARPS = 4;            // epilogue: TMEM read-back (warp w: lanes 32 (w % 4) ..)
+constexpr int TQ_MMA_WARP = TQ_LD_WARPS + TQ_EP_WARPS;  // issues the products (one lane)
+constexpr int TQ_THREADS = (TQ_MMA_WARP + 1) * 32;
+constexpr int TQ_TMEM_COLS = 512;  // F' parts at columns 0, 64, 128; product buffers at 256, 384
+constexpr unsigned TQ_D_COL = 256;
+// mbarriers
+enum {
+  B_XFULL = 0,    // [2] loaders -> MMA: product 1's operand is in X[b]
+  B_X2FULL = 2,   // [2] epilogue -> MMA: product 2's operand is in X[b]
+  B_DFREE = 4,    // [2] epilogue -> MMA: D[b] has been read
+  B_D1 = 6,       // [2] MMA -> epilogue: product 1 is in D[b]
+  B_D2 = 8,       // [2] MMA -> epilogue: product 2 is in D[b]
+  B_XFREE = 10,   // [2] MMA -> loaders: the products reading X[b] are done
+  B_FCOPY = 12,   // the bulk copy of F' into X[1] has landed
+  B_FREADY = 13,  // epilogue -> all: F' is in tensor memory, X[1] is free
+  B_FIN = 14,     // every product issued has completed
+  TQ_NBAR = 15
+};
+constexpr int TQ_SMEM = 2 * TQ_XBUF + TQ_TW_BYTES + TQ_NBAR * 8 + 16;
+static_assert(TQ_SMEM <= 227 * 1024, "radix-4096 pass exceeds the shared memory of a CTA");
+static_assert(3 * FT_PART_BYTES <= TQ_XBUF, "F' staging does not fit an operand buffer");
 
-// issue the six bf16 products D = F' * X (N = TP_N vectors) and commit them to bar
-__device__ __forceinline__ void tc_issue(unsigned char *A, unsigned char *xb, unsigned tmem, unsigned bar) {
-  constexpr unsigned IDESC = idesc_bf16(TC_M, TP_N);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const int pa[6] = {1, 0, 2, 0, 1, 0};
-  const int pb[6] = {1, 2, 0, 1, 0, 0};
-  for (int t = 0; t < 6; t++) {
-    const unsigned abase = smem_addr(A + pa[t] * A_BYTES);
-    const unsigned bbase = smem_addr(xb + pb[t] * X_BYTES);
-#pragma unroll
-    for (int kk = 0; kk < TC_K / 16; kk++) {
-      const unsigned long long ad = smem_desc(abase + kk * 256, 128, (TC_K / 8) * 128);
-      const unsigned long long bd = smem_desc(bbase + kk * 256, 128, (TC_K / 8) * 128);
-      const unsigned acc = (t > 0 || kk > 0) ? 1u : 0u;
-      asm volatile(
-          "{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
-          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem),
-          "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
-          : "memory");
-    }
-  }
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_commit(unsigned bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                : "memory");
 }
 
-// 32 consecutive TMEM columns of this warp's lane quadrant
-__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
-  unsigned r[32];
+// A pipeline wait: gives up at once when another role has given up, else
+// after the engine's bound (and then makes every role give up).  The result
+// is made uniform over the warp, whose TMEM accesses are collective.
+__device__ __forceinline__ bool role_wait(unsigned bar, unsigned parity, volatile int *abort, int *err) {
+  bool ok = *abort == 0;
+  if (ok && !mbar_wait_bounded(bar, parity)) {
+    ok = false;
+    *abort = 1;
+    if (err) atomicExch(err, 1);
+  }
+  return __all_sync(0xffffffffu, ok);
+}
+
+// issue the six bf16 products D = F' * X (A = the F' parts in tensor memory,
+// B = the three parts of X in shared memory, N = TP_N vectors)
+__device__ __forceinline__ void tq_issue(unsigned tmem, unsigned dcol, unsigned xbase) {
+  constexpr unsigned IDESC = idesc_bf16(TC_M, TP_N);
+  const int pa[6] = {1, 0, 2, 0, 1, 0};
+  const int pb[6] = {1, 2, 0, 1, 0, 0};
+#pragma unroll
+  for (int t = 0; t < 6; t++) {
+#pragma unroll
+    for (int kk = 0; kk < TC_K / 16; kk++) {
+      const unsigned at = tmem + (unsigned)(64 * pa[t] + 8 * kk);  // 16 bf16 of K = 8 columns
+      const unsigned long long bd = smem_desc(xbase + pb[t] * X_BYTES + kk * 256, 128, (TC_K / 8) * 128);
+      const unsigned acc = (t > 0 || kk > 0) ? 1u : 0u;
+      asm volatile(
+          "{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p; }" ::"r"(dcol),
+          "r"(at), "l"(bd), "r"(IDESC), "r"(acc)
+          : "memory");
+    }
+  }
+}
+
+// 16 consecutive TMEM columns of this warp's lane quadrant (no wait)
+__device__ __forceinline__ void tmem_ld16_nowait(unsigned taddr, unsigned (&r)[16]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
-      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
-      "%30, %31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 32 consecutive TMEM columns of this warp's lane quadrant from registers
+__device__ __forceinline__ void tmem_st32(unsigned taddr, const unsigned (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, "
+      "%12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31, %32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]),
+      "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]),
+      "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
 }
 
 // three bf16 parts of eight consecutive K values of operand row `row` at
@@ -293,182 +352,284 @@ __device__ __forceinline__ void store_parts8_row(unsigned char *xb, int row, int
 // Product 2's result, lane 2 k1 + c and column (jj, k2), is V[k2 + 64 k1]:
 // each thread pair again exchanges halves so that each thread stores 32
 // consecutive outputs.
-__global__ void __launch_bounds__(TP_THREADS, 1) tc4096_pass_kernel(TcPassArgs a) {
+//
+// The CTA is a two-tile pipeline.  F' lives in tensor memory (the A operand
+// of every product; one bulk copy of the plan's prebuilt parts into X[1],
+// which the epilogue warps move to tensor memory), which leaves shared memory
+// for two operand buffers X[b]
+// and tensor memory for two product buffers D[b]; tile i of the CTA uses
+// buffer b = i & 1.  Loader warps fill X[b] with tile i + 1's operand while
+// the tensor cores and the epilogue warps work on tile i.  The MMA warp
+// issues, in this order, product 1 of tile i and product 2 of tile i - 1; the
+// epilogue warps read back product 1 of tile i (writing product 2's operand
+// into X[b]) and then product 2 of tile i - 1 (storing the outputs).  Every
+// hand-over is an mbarrier, every wait is bounded: a wait that gives up flags
+// the run (a.err) and makes every role stop at its next wait, and the CTA
+// still waits (bounded) for the products it issued before freeing the
+// tensor memory.
+__global__ void __launch_bounds__(TQ_THREADS, 1) tc4096_pass_kernel(TcPassArgs a) {
   extern __shared__ __align__(1024) unsigned char tsm[];
-  unsigned char *A = tsm;                       // 3 parts of F'
-  unsigned char *X = tsm + 3 * A_BYTES;         // 3 parts of the operand of the current product
-  float2 *t4k = reinterpret_cast<float2 *>(tsm + 3 * A_BYTES + 3 * X_BYTES);
-  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tsm + 3 * A_BYTES + 3 * X_BYTES + TW_BYTES);
-  unsigned long long *fbar = bar + 1;
-  unsigned *tmem_slot = reinterpret_cast<unsigned *>(bar + 2);
+  unsigned char *X = tsm;  // X[0], X[1]
+  float2 *tw = reinterpret_cast<float2 *>(tsm + 2 * TQ_XBUF);
+  unsigned long long *bars = reinterpret_cast<unsigned long long *>(tsm + 2 * TQ_XBUF + TQ_TW_BYTES);
+  unsigned *tmem_slot = reinterpret_cast<unsigned *>(bars + TQ_NBAR);
+  volatile int *abort = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quad = warp & 3, half = warp >> 2;
+  const unsigned bar0 = smem_addr(bars);
+#define BAR(i) (bar0 + 8u * (unsigned)(i))
   const float2 *__restrict__ in = reinterpret_cast<const float2 *>(a.in);
   float2 *__restrict__ out = reinterpret_cast<float2 *>(a.out);
   const float2 *__restrict__ twg = reinterpret_cast<const float2 *>(a.tw_R);
   const int logS = a.logN - 12;
   const long long S = 1LL << logS;
+  const long long ntiles = a.total >> 1;
+  const int T = (int)((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x);  // tiles of this CTA
 
-  if (warp == 0) {
+  if (warp == TQ_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
-                 "r"(TP_N)
+                 "r"(TQ_TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(fbar)) : "memory");
+    *abort = 0;
+    for (int b = 0; b < 2; b++) {
+      mbar_init(BAR(B_XFULL + b), TQ_LD_WARPS * 32);
+      mbar_init(BAR(B_X2FULL + b), TQ_EP_WARPS * 32);
+      mbar_init(BAR(B_DFREE + b), TQ_EP_WARPS * 32);
+      mbar_init(BAR(B_D1 + b), 1);
+      mbar_init(BAR(B_D2 + b), 1);
+      mbar_init(BAR(B_XFREE + b), 1);
+    }
+    mbar_init(BAR(B_FCOPY), 1);
+    mbar_init(BAR(B_FREADY), TQ_EP_WARPS * 32);
+    mbar_init(BAR(B_FIN), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(fbar)),
-                 "r"(3 * A_BYTES)
+    // F' (three parts, 96 KiB) into X[1], where the epilogue warps move it to tensor memory
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(BAR(B_FCOPY)),
+                 "r"(3 * FT_PART_BYTES)
                  : "memory");
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_addr(A)),
-        "l"(a.F), "r"(3 * A_BYTES), "r"(smem_addr(fbar))
+            smem_addr(X + TQ_XBUF)),
+        "l"(a.F), "r"(3 * FT_PART_BYTES), "r"(BAR(B_FCOPY))
         : "memory");
   }
-  for (int i = tid; i < 4096; i += TP_THREADS) t4k[i] = twg[i];
+  for (int e = tid; e < 64 * 64; e += TQ_THREADS) tw[e] = twg[((e >> 6) * (e & 63)) & 4095];
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const unsigned tmem = *tmem_slot;
-  const unsigned tq = tmem + ((unsigned)(32 * quad) << 16);  // this warp's lane quadrant
-  const int L = 32 * quad + lane;                             // TMEM lane of this thread
-  const int kc = L >> 1, c = L & 1;                           // output index, Re (0) / Im (1)
-  const int jj = half;                                        // sub-transform of this thread's columns
-  unsigned phase = 0;
-  bool ok = true, f_ready = false;
-  const long long ntiles = (a.total + 1) >> 1;
 
-  for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-    const long long u0 = 2 * t;
-    const bool two = u0 + 1 < a.total;
-    const long long b = u0 >> logS, j = u0 & (S - 1);  // j even: j and j + 1 share a row
-    const float2 *src = in + b * a.bstride + j;
-    // ---- product 1 operand: items (r1, g), r2 = 8 g + q
-#pragma unroll 1
-    for (int it = 0; it < 2; it++) {
-      const int item = tid + it * TP_THREADS;
-      const int r1 = item & 63, g = item >> 6;
-      float4 xv[8];
+  if (warp < TQ_LD_WARPS) {
+    // ---- loaders: items (r1, g) and (r1, g + 4), r2 = 8 g + q
+    const int r1 = tid & 63, g0 = tid >> 6;
+    for (int i = 0; i < T; i++) {
+      const int b = i & 1;
+      const unsigned u = (unsigned)i >> 1;
+      bool ok = true;
+      if (i == 1) ok = role_wait(BAR(B_FREADY), 0, abort, a.err);  // X[1] held the F' copy
+      if (ok && u > 0) ok = role_wait(BAR(B_XFREE + b), (u - 1) & 1, abort, a.err);
+      if (!ok) break;
+      const long long u0 = 2 * ((long long)blockIdx.x + (long long)i * gridDim.x);
+      const long long row = u0 >> logS, j = u0 & (S - 1);  // j even: j and j + 1 share a row
+      const float2 *src = in + row * a.bstride + j;
+      float4 xv[2][8];
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const long long off = (long long)(r1 + 64 * (8 * g + q)) << logS;
-        if (two) {
-          xv[q] = *reinterpret_cast<const float4 *>(src + off);
-        } else {
-          const float2 v = src[off];
-          xv[q] = make_float4(v.x, v.y, 0.f, 0.f);
-        }
-      }
+      for (int h = 0; h < 2; h++)
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          xv[h][q] = __ldg(reinterpret_cast<const float4 *>(
+              src + ((long long)(r1 + 64 * (8 * (g0 + 4 * h) + q)) << logS)));
       for (int s2 = 1; s2 < a.nsum; s2++) {
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-          const long long off = s2 * a.sstride + ((long long)(r1 + 64 * (8 * g + q)) << logS);
-          float4 v;
-          if (two) {
-            v = *reinterpret_cast<const float4 *>(src + off);
-          } else {
-            const float2 w = src[off];
-            v = make_float4(w.x, w.y, 0.f, 0.f);
+        for (int h = 0; h < 2; h++)
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(
+                src + s2 * a.sstride + ((long long)(r1 + 64 * (8 * (g0 + 4 * h) + q)) << logS)));
+            xv[h][q].x += v.x;
+            xv[h][q].y += v.y;
+            xv[h][q].z += v.z;
+            xv[h][q].w += v.w;
           }
-          xv[q].x += v.x;
-          xv[q].y += v.y;
-          xv[q].z += v.z;
-          xv[q].w += v.w;
-        }
       }
-      float re0[8], im0[8], re1[8], im1[8];
+      unsigned char *xb = X + b * TQ_XBUF;
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        re0[q] = xv[q].x;
-        im0[q] = a.inverse ? -xv[q].y : xv[q].y;
-        re1[q] = xv[q].z;
-        im1[q] = a.inverse ? -xv[q].w : xv[q].w;
+      for (int h = 0; h < 2; h++) {
+        const int g = g0 + 4 * h;
+        float re0[8], im0[8], re1[8], im1[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          re0[q] = xv[h][q].x;
+          im0[q] = a.inverse ? -xv[h][q].y : xv[h][q].y;
+          re1[q] = xv[h][q].z;
+          im1[q] = a.inverse ? -xv[h][q].w : xv[h][q].w;
+        }
+        store_parts8_row(xb, r1, 8 * g, re0);
+        store_parts8_row(xb, r1, 64 + 8 * g, im0);
+        store_parts8_row(xb, 64 + r1, 8 * g, re1);
+        store_parts8_row(xb, 64 + r1, 64 + 8 * g, im1);
       }
-      store_parts8_row(X, r1, 8 * g, re0);
-      store_parts8_row(X, r1, 64 + 8 * g, im0);
-      store_parts8_row(X, 64 + r1, 8 * g, re1);
-      store_parts8_row(X, 64 + r1, 64 + 8 * g, im1);
-    }
-    for (int step = 0; step < 2 && ok; step++) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
-        bool go = true;
-        if (!f_ready) {
-          go = mbar_wait_bounded(smem_addr(fbar), 0);
-          f_ready = go;
-        }
-        if (go) {
-          tc_issue(A, X, tmem, smem_addr(bar));
-        } else {
-          // nothing issued: arrive on the barrier so that every thread leaves its wait
-          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-          ok = false;
-          if (a.err) atomicExch(a.err, 1);
-        }
-      }
-      if (!mbar_wait_bounded(smem_addr(bar), phase)) {
-        ok = false;
-        if (tid == 0 && a.err) atomicExch(a.err, 1);
-      }
-      ok = __syncthreads_and(ok) != 0;  // warp-collective TMEM loads below: all or none
-      phase ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      if (!ok) break;
-      if (step == 0) {
-        // D1 lane (kc = k2, c), columns n = 64 jj + r1  ->  product 2 operand
+      mbar_arrive(BAR(B_XFULL + b));
+    }
+  } else if (warp < TQ_MMA_WARP) {
+    // ---- epilogue: TMEM lane L = 32 q + lane
+    const int q = warp & 3;
+    const int L = 32 * q + lane;
+    const int kc = L >> 1, c = L & 1;
+    const unsigned tq = tmem + ((unsigned)(32 * q) << 16);
+    bool ok = role_wait(BAR(B_FCOPY), 0, abort, a.err);
+    if (ok) {
+      // F' row L of each part: shared staging -> tensor memory columns 64 p + 32 h ..
+      const unsigned char *fs = X + TQ_XBUF;
 #pragma unroll 1
-        for (int c0 = 0; c0 < 64; c0 += 32) {
-          float y[32];
-          tmem_ld32(tq + (unsigned)(64 * jj + c0), y);
-          float z[32];
+      for (int p = 0; p < 3; p++)
+#pragma unroll 1
+        for (int h = 0; h < 2; h++) {
+          unsigned r[32];
 #pragma unroll
-          for (int i = 0; i < 32; i++) {
-            const float other = __shfl_xor_sync(0xffffffffu, y[i], 1);
-            const float yr = c ? other : y[i], yi = c ? y[i] : other;
-            const float2 w = t4k[((c0 + i) * kc) & 4095];
+          for (int cc = 0; cc < 8; cc++) {
+            const int ch = 8 * h + cc;
+            const uint4 v = *reinterpret_cast<const uint4 *>(fs + p * FT_PART_BYTES + L * FT_ROW_BYTES +
+                                                             ((ch ^ (L & 15)) << 4));
+            r[4 * cc] = v.x;
+            r[4 * cc + 1] = v.y;
+            r[4 * cc + 2] = v.z;
+            r[4 * cc + 3] = v.w;
+          }
+          tmem_st32(tq + (unsigned)(64 * p + 32 * h), r);
+        }
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(BAR(B_FREADY));
+    }
+    for (int s = 0; s <= T && ok; s++) {
+      if (s < T) {
+        // product 1 of tile s -> product 2's operand in X[b]
+        const int b = s & 1;
+        const unsigned u = (unsigned)s >> 1;
+        ok = role_wait(BAR(B_D1 + b), u & 1, abort, a.err);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        unsigned char *xb = X + b * TQ_XBUF;
+        const unsigned dcol = tq + TQ_D_COL + 128u * b;
+#pragma unroll 1
+        for (int n0 = 0; n0 < 128; n0 += 16) {  // columns n = 64 jj + r1
+          const int jj = n0 >> 6, c0 = n0 & 63;
+          unsigned yr_[16];
+          tmem_ld16_nowait(dcol + (unsigned)n0, yr_);
+          tmem_wait_ld();
+          float z[16];
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            const float y = __uint_as_float(yr_[i]);
+            const float other = __shfl_xor_sync(0xffffffffu, y, 1);
+            const float yr = c ? other : y, yi = c ? y : other;
+            const float2 w = tw[(c0 + i) * 64 + kc];
             z[i] = c ? fmaf(yr, w.y, yi * w.x) : fmaf(yr, w.x, -(yi * w.y));
           }
-#pragma unroll
-          for (int grp = 0; grp < 4; grp++)
-            store_parts8_row(X, 64 * jj + kc, (c ? 64 : 0) + c0 + 8 * grp, z + 8 * grp);
+          store_parts8_row(xb, 64 * jj + kc, (c ? 64 : 0) + c0, z);
+          store_parts8_row(xb, 64 * jj + kc, (c ? 64 : 0) + c0 + 8, z + 8);
         }
-      } else if (jj == 0 || two) {
-        // D3 lane (kc = k1, c), columns (jj, k2): V[k2 + 64 k1]; this thread keeps k2 in [32 c, 32 c + 32)
-        float2 v[32];
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(BAR(B_X2FULL + b));
+      }
+      if (s >= 1) {
+        // product 2 of tile s - 1 -> outputs
+        const int i = s - 1, b = i & 1;
+        const unsigned u = (unsigned)i >> 1;
+        ok = role_wait(BAR(B_D2 + b), u & 1, abort, a.err);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const unsigned dcol = tq + TQ_D_COL + 128u * b;
+        const long long u0 = 2 * ((long long)blockIdx.x + (long long)i * gridDim.x);
+        const long long row = u0 >> logS, j = u0 & (S - 1);
+        const float sg = a.inverse ? -1.f : 1.f;
 #pragma unroll 1
-        for (int c0 = 0; c0 < 64; c0 += 32) {
-          float y[32];
-          tmem_ld32(tq + (unsigned)(64 * jj + c0), y);
-          const bool keep = c0 == 32 * c;
+        for (int n0 = 0; n0 < 128; n0 += 64) {
+          // lane (kc = k1, c), columns n0 + k2: V[k2 + 64 k1] of sub-transform jj = n0 / 64.
+          // Thread c keeps k2 in [32 c, 32 c + 32): its own half (Re for c = 0,
+          // Im for c = 1) of those columns and its partner's other half.
+          const int jj = n0 >> 6;
+          float2 *dp = out + row * a.bstride + (j + jj) * 4096 + 64 * kc + 32 * c;
+#pragma unroll 1
+          for (int h = 0; h < 32; h += 16) {
+            unsigned ya[16], yb[16];
+            tmem_ld16_nowait(dcol + (unsigned)(n0 + h), ya);       // k2 = h ..
+            tmem_ld16_nowait(dcol + (unsigned)(n0 + 32 + h), yb);  // k2 = 32 + h ..
+            tmem_wait_ld();
 #pragma unroll
-          for (int i = 0; i < 32; i++) {
-            const float other = __shfl_xor_sync(0xffffffffu, y[i], 1);
-            if (keep) v[i] = c ? make_float2(other, y[i]) : make_float2(y[i], other);
+            for (int i2 = 0; i2 < 16; i2 += 2) {
+              float re[2], im[2];
+#pragma unroll
+              for (int e = 0; e < 2; e++) {
+                const float send = __uint_as_float(c ? ya[i2 + e] : yb[i2 + e]);
+                const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+                const float own = __uint_as_float(c ? yb[i2 + e] : ya[i2 + e]);
+                re[e] = c ? recv : own;
+                im[e] = sg * (c ? own : recv);
+              }
+              *reinterpret_cast<float4 *>(dp + h + i2) = make_float4(re[0], im[0], re[1], im[1]);
+            }
           }
         }
-        float2 *dp = out + b * a.bstride + (j + jj) * 4096 + 64 * kc + 32 * c;
-#pragma unroll
-        for (int i = 0; i < 32; i += 2) {
-          const float s = a.inverse ? -1.f : 1.f;
-          *reinterpret_cast<float4 *>(dp + i) = make_float4(v[i].x, s * v[i].y, v[i + 1].x, s * v[i + 1].y);
-        }
-      } else {
-        // the second sub-transform of a tile with one: no outputs, but the
-        // warp still took part in the collective loads of the other half
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(BAR(B_DFREE + b));
       }
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // the operand buffer and TMEM are rewritten by the next tile
+  } else {
+    // ---- MMA warp: product 1 of tile s, then product 2 of tile s - 1
+    bool ok = role_wait(BAR(B_FREADY), 0, abort, a.err);
+    bool issued = false;
+    for (int s = 0; s <= T && ok; s++) {
+      if (s < T) {
+        const int b = s & 1;
+        const unsigned u = (unsigned)s >> 1;
+        ok = role_wait(BAR(B_XFULL + b), u & 1, abort, a.err);
+        if (ok && u > 0) ok = role_wait(BAR(B_DFREE + b), (u - 1) & 1, abort, a.err);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (lane == 0) {
+          tq_issue(tmem, tmem + TQ_D_COL + 128u * b, smem_addr(X + b * TQ_XBUF));
+          tc_commit(BAR(B_D1 + b));
+        }
+        __syncwarp();
+        issued = true;
+      }
+      if (s >= 1) {
+        const int i = s - 1, b = i & 1;
+        const unsigned u = (unsigned)i >> 1;
+        ok = role_wait(BAR(B_X2FULL + b), u & 1, abort, a.err);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (lane == 0) {
+          tq_issue(tmem, tmem + TQ_D_COL + 128u * b, smem_addr(X + b * TQ_XBUF));
+          tc_commit(BAR(B_D2 + b));
+          tc_commit(BAR(B_XFREE + b));
+        }
+        __syncwarp();
+      }
+    }
+    if (lane == 0) {
+      if (issued) {
+        tc_commit(BAR(B_FIN));
+        if (!mbar_wait_bounded(BAR(B_FIN), 0) && a.err) atomicExch(a.err, 1);
+      }
+      // the F' copy has landed (a no-op unless a wait gave up before it)
+      (void)mbar_wait_bounded(BAR(B_FCOPY), 0);
+    }
+    __syncwarp();
   }
-  if (tid == 0 && !f_ready) (void)mbar_wait_bounded(smem_addr(fbar), 0);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP_N) : "memory");
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == TQ_MMA_WARP)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TQ_TMEM_COLS)
+                 : "memory");
+#undef BAR
 }
 
 }  // namespace
@@ -517,22 +678,23 @@ int launch_bounded_wait_probe(long long limit, int *gave_up, cudaStream_t st) {
 }
 
 int tc_build_F(void **F) {
-  GS_CUDA(cudaMalloc(F, 3 * A_BYTES));
-  tc_build_F_kernel<<<(TC_M * TC_K + 255) / 256, 256>>>(static_cast<unsigned char *>(*F));
+  GS_CUDA(cudaMalloc(F, 3 * FT_PART_BYTES));
+  tc_build_F_kernel<<<(TC_M * (TC_K / 2) + 255) / 256, 256>>>(static_cast<unsigned char *>(*F));
   GS_LAUNCHED();
   return GSFFT_OK;
 }
 
 int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st) {
-  // first passes only (Ns = 1, outputs contiguous per sub-transform), an even
-  // number of sub-transforms per row and 16-byte aligned element pairs
+  // first passes only (Ns = 1, outputs contiguous per sub-transform), at
+  // least two sub-transforms per row (so a tile's pair shares a row) and
+  // 16-byte aligned element pairs
   if (a.logNs != 0 || a.logN < 13 || !a.tw_R || !a.F || a.samples || a.row_max || !a.write_complex)
     return GSFFT_ERR_UNSUPPORTED;
   if ((reinterpret_cast<uintptr_t>(a.in) & 15) || (reinterpret_cast<uintptr_t>(a.out) & 15) ||
-      (a.bstride & 1) || (a.nsum > 1 && (a.sstride & 1)))
+      (a.bstride & 1) || (a.nsum > 1 && (a.sstride & 1)) || a.nsum < 1 || (a.total & 1))
     return GSFFT_ERR_UNSUPPORTED;
   static PerContext<int> attr;  // the kernel's dynamic shared memory limit, per context
-  GS_CHECK(attr.ensure_at_least(TC4K_SMEM, [](int v) {
+  GS_CHECK(attr.ensure_at_least(TQ_SMEM, [](int v) {
     if (cudaFuncSetAttribute(tc4096_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v) ==
         cudaSuccess)
       return (int)GSFFT_OK;
@@ -543,10 +705,12 @@ int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st) {
   int dev = 0, sms = 0;
   GS_CUDA(cudaGetDevice(&dev));
   GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const long long ntiles = (a.total + 1) / 2;
-  const int grid = (int)(ntiles < sms ? ntiles : sms);
+  // one CTA per SM (its shared memory allows no second), so that each holds
+  // all 512 tensor-memory columns of its SM
+  const long long ntiles = a.total / 2;
+  const long long grid = ntiles < sms ? ntiles : sms;
   if (grid < 1) return GSFFT_OK;
-  tc4096_pass_kernel<<<grid, TP_THREADS, TC4K_SMEM, st>>>(a);
+  tc4096_pass_kernel<<<(int)grid, TQ_THREADS, TQ_SMEM, st>>>(a);
   GS_LAUNCHED();
   return GSFFT_OK;
 }

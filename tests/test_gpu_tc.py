@@ -63,10 +63,14 @@ def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
 
 
 @pytest.mark.parametrize("n,batch,sign", [(1 << 17, 9, -1), (1 << 20, 2, -1), (1 << 22, 2, -1),
-                                          (1 << 17, 1, 1)])
+                                          (1 << 17, 1, 1), (1 << 17, 3, -1), (1 << 22, 5, -1),
+                                          (1 << 20, 3, 1)])
 def test_tc_fft_matches_numpy(G, torch_cuda, n, batch, sign):
     """The FP32 FFT whose radix-4096 first pass runs on the tensor cores (the
-    bucket FFT's B = 2^17 shape and the RLFC FFT's W = 2^22 shape)."""
+    bucket FFT's B = 2^17 shape and the RLFC FFT's W = 2^22 shape).  The
+    pass is a two-tile pipeline per CTA: 2^17 x 3 gives one tile to each of
+    48 CTAs, 2^22 x 5 about 34 tiles to each CTA (both buffers reused many
+    times), 2^22 x 2 an odd number to some."""
     torch = torch_cuda
     rng = np.random.default_rng(n + batch)
     x = (rng.normal(size=(batch, n)) + 1j * rng.normal(size=(batch, n))).astype(np.complex64)
