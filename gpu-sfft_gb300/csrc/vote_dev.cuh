@@ -128,6 +128,119 @@ __device__ __forceinline__ unsigned warp_excl_scan(unsigned v, unsigned *total) 
 constexpr int WPB = VT / 32;  // buckets (warps) per block
 constexpr int STASH = 32;     // candidates recorded per heavy bucket by the count pass
 
+// Votes of heavy bucket t (one warp): returns this lane's number of visited
+// positions whose count reached the threshold, and records the bucket's
+// first STASH of them, in window order, at slot[] (global or shared memory).
+__device__ __forceinline__ unsigned count_walk(const WalkArgs &w, int t, unsigned epoch, unsigned thresh,
+                                               unsigned *vote, int *slot) {
+  const unsigned nmask = (unsigned)w.n - 1u;
+  unsigned c = 0;
+  unsigned recorded = 0;  // this bucket's candidates so far (warp-uniform)
+  for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
+    // up to four visited positions at a time: their table reads are
+    // independent, so they overlap instead of paying one DRAM latency each
+    unsigned app = 0;  // bits of this lane's mask whose count reached the threshold
+    while (mask) {
+      unsigned loc[4], e[4];
+      int nq = 0;
+      const unsigned before = mask;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (mask) {
+          const int bq = __ffs(mask) - 1;
+          mask &= mask - 1;
+          loc[q] = ((unsigned)pos(bq) * w.a) & nmask;
+          nq = q + 1;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (q < nq) e[q] = __ldcg(&vote[loc[q]]);
+      unsigned hitq = 0;  // bit q: position q of this round reached the threshold
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (q < nq) {
+          const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
+          vote[loc[q]] = (epoch << 8) | cv;
+          hitq |= (unsigned)(cv == thresh) << q;
+        }
+      }
+      // the round's positions are the lowest set bits of `before`, in order
+      unsigned taken = before & ~mask;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const unsigned low = taken & (0u - taken);
+        taken ^= low;
+        if ((hitq >> q) & 1u) app |= low;
+      }
+    }
+    c += (unsigned)__popc(app);
+    // window order: chunks, then lanes, then bits (as the write pass walks)
+    if (__any_sync(0xffffffffu, app != 0u)) {
+      unsigned ctot;
+      unsigned o = recorded + warp_excl_scan((unsigned)__popc(app), &ctot);
+      while (app) {
+        const int b = __ffs(app) - 1;
+        app &= app - 1;
+        if (o < (unsigned)STASH) slot[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
+        o++;
+      }
+      recorded += ctot;
+    }
+  });
+  return c;
+}
+
+// Appends heavy bucket t's cw candidates (warp-uniform) at cand[next ..]:
+// copied from slot[] when the count walk recorded them all (GLOBAL_SLOT: the
+// slots were written by another launch or block, so the loads bypass L1),
+// else found again by walking the window and the vote table.
+template <bool GLOBAL_SLOT>
+__device__ __forceinline__ void write_bucket(const WalkArgs &w, int t, unsigned epoch, unsigned thresh,
+                                             const unsigned *vote, unsigned cw, const int *slot,
+                                             int *cand, int cap, long long next) {
+  const int lane = threadIdx.x & 31;
+  if (cw <= (unsigned)STASH) {
+    for (unsigned j = lane; j < cw; j += 32) {
+      const long long o = next + j;
+      if (o < cap) cand[o] = GLOBAL_SLOT ? __ldcg(&slot[j]) : slot[j];
+    }
+    return;
+  }
+  const unsigned nmask = (unsigned)w.n - 1u;
+  const unsigned want = (epoch << 8) | thresh;
+  for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
+    // appended positions of this lane, in bit order
+    unsigned app = 0;
+    unsigned m = mask;
+    while (m) {
+      unsigned loc[4], bit[4];
+      int nq = 0;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (m) {
+          bit[q] = __ffs(m) - 1;
+          m &= m - 1;
+          loc[q] = ((unsigned)pos((int)bit[q]) * w.a) & nmask;
+          nq = q + 1;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (q < nq && __ldcg(&vote[loc[q]]) == want) app |= 1u << bit[q];
+    }
+    unsigned ctot;
+    long long o = next + warp_excl_scan((unsigned)__popc(app), &ctot);
+    while (app) {
+      const int b = __ffs(app) - 1;
+      app &= app - 1;
+      if (o < cap) cand[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
+      o++;
+    }
+    next += ctot;
+  });
+}
+
 // One block of the count pass (block bid of nblk): votes of the location
 // loop, each bucket's candidate count and first STASH candidates; the last
 // block to finish writes the exclusive scan of the block counts.
@@ -139,63 +252,7 @@ __device__ __forceinline__ void vote_count_block(const WalkArgs &w, unsigned epo
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int t = bid * WPB + warp;
   unsigned c = 0;
-  if (t < w.Bt) {
-    const unsigned nmask = (unsigned)w.n - 1u;
-    int *const slot = stash + (size_t)t * STASH;
-    unsigned recorded = 0;  // this bucket's candidates so far (warp-uniform)
-    for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
-      // up to four visited positions at a time: their table reads are
-      // independent, so they overlap instead of paying one DRAM latency each
-      unsigned app = 0;  // bits of this lane's mask whose count reached the threshold
-      while (mask) {
-        unsigned loc[4], e[4];
-        int nq = 0;
-        const unsigned before = mask;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (mask) {
-            const int bq = __ffs(mask) - 1;
-            mask &= mask - 1;
-            loc[q] = ((unsigned)pos(bq) * w.a) & nmask;
-            nq = q + 1;
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-          if (q < nq) e[q] = __ldcg(&vote[loc[q]]);
-        unsigned hitq = 0;  // bit q: position q of this round reached the threshold
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (q < nq) {
-            const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
-            vote[loc[q]] = (epoch << 8) | cv;
-            hitq |= (unsigned)(cv == thresh) << q;
-          }
-        }
-        // the round's positions are the lowest set bits of `before`, in order
-        unsigned taken = before & ~mask;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const unsigned low = taken & (0u - taken);
-          taken ^= low;
-          if ((hitq >> q) & 1u) app |= low;
-        }
-      }
-      c += (unsigned)__popc(app);
-      // window order: chunks, then lanes, then bits (as the write pass walks)
-      if (__any_sync(0xffffffffu, app != 0u)) {
-        unsigned ctot;
-        unsigned o = recorded + warp_excl_scan((unsigned)__popc(app), &ctot);
-        while (app) {
-          const int b = __ffs(app) - 1;
-          app &= app - 1;
-          if (o < (unsigned)STASH) slot[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
-          o++;
-        }
-        recorded += ctot;
-      }
-    });
-  }
+  if (t < w.Bt) c = count_walk(w, t, epoch, thresh, vote, stash + (size_t)t * STASH);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
   if (lane == 0 && t < w.Bt) cnt[t] = (int)c;
@@ -282,47 +339,7 @@ __device__ __forceinline__ void vote_write_block(const WalkArgs &w, unsigned epo
   const unsigned wpre = blk_excl_scan(c, ws, &tot);  // lane 0 of each warp carries its count
   long long next = (long long)base_prev + __ldcg(&blk_pre[bid]) + __shfl_sync(0xffffffffu, wpre, 0);
   const unsigned cw = __shfl_sync(0xffffffffu, c, 0);
-  if (cw && cw <= (unsigned)STASH) {
-    // recorded by the count pass in window order
-    const int *slot = stash + (size_t)t * STASH;
-    for (unsigned j = lane; j < cw; j += 32) {
-      const long long o = next + j;
-      if (o < cap) cand[o] = __ldcg(&slot[j]);
-    }
-  } else if (cw) {
-    const unsigned nmask = (unsigned)w.n - 1u;
-    const unsigned want = (epoch << 8) | thresh;
-    for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
-      // appended positions of this lane, in bit order
-      unsigned app = 0;
-      unsigned m = mask;
-      while (m) {
-        unsigned loc[4], bit[4];
-        int nq = 0;
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (m) {
-            bit[q] = __ffs(m) - 1;
-            m &= m - 1;
-            loc[q] = ((unsigned)pos((int)bit[q]) * w.a) & nmask;
-            nq = q + 1;
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-          if (q < nq && __ldcg(&vote[loc[q]]) == want) app |= 1u << bit[q];
-      }
-      unsigned ctot;
-      long long o = next + warp_excl_scan((unsigned)__popc(app), &ctot);
-      while (app) {
-        const int b = __ffs(app) - 1;
-        app &= app - 1;
-        if (o < cap) cand[o] = (int)(((unsigned)pos(b) * w.a) & nmask);
-        o++;
-      }
-      next += ctot;
-    });
-  }
+  if (cw) write_bucket<true>(w, t, epoch, thresh, vote, cw, stash + (size_t)t * STASH, cand, cap, next);
   // the last block to finish publishes the new candidate count; every block
   // read the old one before its thread 0 takes a ticket (barrier + fence)
   __syncthreads();
