@@ -78,7 +78,10 @@ __device__ __forceinline__ void stage_of(const TailPlan &tp, int s, int *kind, i
   *loop = marks + r / 2;
 }
 
-__global__ void __launch_bounds__(VT)
+// Eight CTAs per SM (32 registers): the walks are chains of dependent L2 and
+// DRAM reads, so warps in flight set the pace (measured on 256 mixed signals:
+// 6.27 ms per batch at 4 CTAs per SM, 6.00 at 6, 5.76 at 8).
+__global__ void __launch_bounds__(VT, 8)
 batch_tail_kernel(const TailPlan *__restrict__ plans, const TailRange *__restrict__ ranges,
                   const int *__restrict__ item_range, int total, int *queue, int *done, int *err) {
   __shared__ int s_item, s_range;

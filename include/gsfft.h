@@ -235,7 +235,9 @@ int gsfft_batch_launch(gsfft_batch batch, void *stream);
  * stage order, with bounded waits that end in GSFFT_ERR_TIMEOUT), then every
  * plan's estimation and top-k on its stream.  Results equal the plans' single
  * runs.  Plans with at most 16 location loops (GSFFT_ERR_UNSUPPORTED
- * otherwise).  Drops a captured graph; on = 0 returns to per-plan voting. */
+ * otherwise).  Drops a captured graph; on = 0 returns to per-plan voting.
+ * Off by default; on 256 small signals it measured 5.96 ms per batch against
+ * 6.26 ms with per-plan voting (tuned, 64 streams). */
 int gsfft_batch_set_persistent_tail(gsfft_batch batch, int on);
 
 /* ---- host I/O and evaluation ---------------------------------------- */
