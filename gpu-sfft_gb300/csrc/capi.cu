@@ -413,11 +413,12 @@ int gsfft_check_bounded_wait(long long limit_cycles, void *stream) {
   return GSFFT_OK;
 }
 
-int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
-                 void *stream) {
+// an FP32 FFT with one of the tensor-core plans (its completion waits checked)
+static int fft_tc_run(int (*init)(FftPlan &, long long, int), const char *what, const void *d_in,
+                      void *d_out, long long n_fft, int batch, int sign, void *stream) {
   if (!d_in || !d_out || batch < 1 || (sign != 1 && sign != -1)) return GSFFT_ERR_PARAM;
   FftPlan fp;
-  int s = fft_plan_init_tc(fp, n_fft, batch);
+  int s = init(fp, n_fft, batch);
   if (s == GSFFT_OK) {
     int *err = nullptr;
     if (cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
@@ -431,11 +432,11 @@ int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int 
       if (s == GSFFT_OK &&
           (cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, S(stream)) != cudaSuccess ||
            cudaStreamSynchronize(S(stream)) != cudaSuccess)) {
-        set_last_error("gsfft_fft_tc: %s", cudaGetErrorString(cudaGetLastError()));
+        set_last_error("%s: %s", what, cudaGetErrorString(cudaGetLastError()));
         s = GSFFT_ERR_CUDA;
       }
       if (s == GSFFT_OK && h) {
-        set_last_error("gsfft_fft_tc: a tensor-core completion wait timed out");
+        set_last_error("%s: a tensor-core completion wait timed out", what);
         s = GSFFT_ERR_TIMEOUT;
       }
       cudaFree(err);
@@ -443,6 +444,16 @@ int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int 
   }
   fft_plan_free(fp);
   return s;
+}
+
+int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
+                 void *stream) {
+  return fft_tc_run(fft_plan_init_tc, "gsfft_fft_tc", d_in, d_out, n_fft, batch, sign, stream);
+}
+
+int gsfft_fft_tc64(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
+                   void *stream) {
+  return fft_tc_run(fft_plan_init_tc64, "gsfft_fft_tc64", d_in, d_out, n_fft, batch, sign, stream);
 }
 
 int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precision, int *d_out,

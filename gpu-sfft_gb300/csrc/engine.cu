@@ -177,8 +177,12 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   P->floor_rel = (flags & GSFFT_FLAG_RAW_SELECTION) ? 0.0 : 1e-10;
   if (s == GSFFT_OK) {
     int t = GSFFT_ERR_UNSUPPORTED;
-    if (precision == GSFFT_MIXED && (flags & GSFFT_FLAG_TC_BUCKET_FFT))
-      t = fft_plan_init_tc(P->fftB, p.B, p.loops);
+    // tensor-core bucket FFT: the radix-64 last pass where B allows it
+    // (2^13 .. 2^20), else the radix-4096 first pass
+    if (precision == GSFFT_MIXED && (flags & GSFFT_FLAG_TC_BUCKET_FFT)) {
+      t = fft_plan_init_tc64(P->fftB, p.B, p.loops);
+      if (t == GSFFT_ERR_UNSUPPORTED) t = fft_plan_init_tc(P->fftB, p.B, p.loops);
+    }
     P->tc_bucket = t == GSFFT_OK;
     if (!P->tc_bucket) s = fft_plan_init(P->fftB, p.B, precision, p.loops, tn.bucket_first_radix);
   }

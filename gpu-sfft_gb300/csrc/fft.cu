@@ -137,6 +137,44 @@ int fft_plan_init_tc(FftPlan &p, long long n, int max_batch) {
   return GSFFT_OK;
 }
 
+// FP32 plan whose first pass is a CUDA-core pass of radix 2^(L-6) and whose
+// last pass is a tensor-core radix-64 pass (one DFT_64 product per 128
+// sub-transforms, both sides read and written in 1 KiB runs): n = 2^L,
+// 13 <= L <= 20.
+int fft_plan_init_tc64(FftPlan &p, long long n, int max_batch) {
+  fft_plan_free(p);
+  if (n < 256 || (n & (n - 1)) != 0) return GSFFT_ERR_UNSUPPORTED;
+  int L = 0;
+  while ((1LL << L) < n) L++;
+  if (L < 13 || L > 20) return GSFFT_ERR_UNSUPPORTED;
+  p.n = n;
+  p.L = L;
+  p.precision = GSFFT_MIXED;
+  p.npass = 2;
+  p.logR[0] = L - 6;
+  p.logR[1] = 6;
+  p.tc[0] = false;
+  p.tc[1] = true;
+  long long Np = 1;
+  for (int i = 0; i < p.npass; i++) {
+    const long long R = 1LL << p.logR[i];
+    Np *= R;
+    int lg = 0;
+    while ((1LL << lg) < Np) lg++;
+    const int h = (lg + 1) / 2;
+    p.tw_h[i] = h;
+    const long long nlo = 1LL << h, nhi = (Np + nlo - 1) / nlo;
+    GS_CHECK(make_table<float>(&p.tw_lo[i], nlo, 1, Np));
+    GS_CHECK(make_table<float>(&p.tw_hi[i], nhi, nlo, Np));
+    GS_CHECK(make_table<float>(&p.tw_R[i], R, 1, R));
+  }
+  GS_CHECK(tc_build_F_smem(&p.tc_F));
+  p.scratch_elems = (long long)n * max_batch;
+  GS_CUDA(cudaMalloc(&p.scratch, sizeof(float2) * p.scratch_elems));
+  GS_CUDA(cudaDeviceSynchronize());
+  return GSFFT_OK;
+}
+
 void fft_plan_free(FftPlan &p) {
   for (int i = 0; i < 3; i++) {
     if (p.tw_hi[i]) cudaFree(p.tw_hi[i]);
@@ -200,7 +238,7 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
     a.total = total_sub;
     int s;
     if (p.tc[i]) {
-      if (dbl || a.gx || p.logR[i] != 12) return GSFFT_ERR_UNSUPPORTED;  // partial sums, no gather
+      if (dbl || a.gx || (p.logR[i] != 12 && p.logR[i] != 6)) return GSFFT_ERR_UNSUPPORTED;
       TcPassArgs t;
       t.in = a.in;
       t.out = a.out;
@@ -220,7 +258,7 @@ int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,
       t.err = io.err;
       t.nsum = a.nsum;
       t.sstride = a.sstride;
-      s = launch_tc4096_pass(t, st);
+      s = p.logR[i] == 6 ? launch_tc64_last_pass(t, st) : launch_tc4096_pass(t, st);
     } else {
       s = dispatch_pass(dbl, p.logR[i], a, total_sub, st);
     }

@@ -224,8 +224,12 @@ struct TcPassArgs {
   int *err;             // set when a completion wait timed out (may be null)
   int nsum = 1;         // radix-4096 form: add nsum partial inputs sstride apart
   long long sstride = 0;
+  int max_ctas = 0;     // grid cap (0: one CTA per SM)
 };
 int tc_build_F(void **F);
+// radix 64 as the last pass (one DFT_64 product per 128 sub-transforms)
+int tc_build_F_smem(void **F);
+int launch_tc64_last_pass(const TcPassArgs &a, cudaStream_t st);
 // radix 4096 = 64 x 64 in one pass (four-step, both DFT_64 stages on the tensor cores)
 int launch_tc4096_pass(const TcPassArgs &a, cudaStream_t st);
 
@@ -254,6 +258,8 @@ int fft_plan_init(FftPlan &p, long long n, int precision, int max_batch, int fir
 // FP32 plan: radix-4096 tensor-core pass, then a CUDA-core pass of radix
 // n / 4096; GSFFT_ERR_UNSUPPORTED unless n = 2^(17..26)
 int fft_plan_init_tc(FftPlan &p, long long n, int max_batch);
+// FP32 plan: CUDA-core radix-2^(L-6) first pass, tensor-core radix-64 last pass (13 <= L <= 20)
+int fft_plan_init_tc64(FftPlan &p, long long n, int max_batch);
 void fft_plan_free(FftPlan &p);
 // in: batch entries at in + b*n; out: out + b*n.  sign -1 forward, +1 inverse.
 int fft_exec(const FftPlan &p, const void *in, void *out, int batch, int sign,

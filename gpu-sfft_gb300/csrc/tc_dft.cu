@@ -632,6 +632,217 @@ __global__ void __launch_bounds__(TQ_THREADS, 1) tc4096_pass_kernel(TcPassArgs a
 #undef BAR
 }
 
+// ---- radix-64 last pass ----------------------------------------------------
+// The three bf16 parts of F' (as above: interleaved Re / Im rows) in the
+// shared-memory layout of an A operand (K-major, no swizzle), 3 x 32 KiB.
+__global__ void tc_build_F_smem_kernel(unsigned char *F) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= TC_M * TC_K) return;
+  const int m = e / TC_K, k = e % TC_K;
+  const int o = m >> 1, i = k & 63;
+  double sn, cs;
+  sincospi(2.0 * (double)((o * i) & 63) / 64.0, &sn, &cs);
+  float f;
+  if ((m & 1) == 0) f = (k < 64) ? (float)cs : (float)sn;
+  else f = (k < 64) ? (float)(-sn) : (float)cs;
+  __nv_bfloat16 p0, p1, p2;
+  split3(f, p0, p1, p2);
+  const int off = kmajor_off(m, k, TC_K);
+  *reinterpret_cast<__nv_bfloat16 *>(F + off) = p0;
+  *reinterpret_cast<__nv_bfloat16 *>(F + A_BYTES + off) = p1;
+  *reinterpret_cast<__nv_bfloat16 *>(F + 2 * A_BYTES + off) = p2;
+}
+
+constexpr int T64_THREADS = 256;  // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. + 31
+constexpr int T64_SMEM = 3 * A_BYTES + 3 * X_BYTES + 64;
+static_assert(T64_SMEM <= 227 * 1024, "radix-64 pass exceeds the shared memory of a CTA");
+
+__device__ __forceinline__ float sq_sum_f(float x, float y) { return __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)); }
+
+// The last Stockham pass (radix 64, Ns = S = N / 64) of an FP32 FFT on the
+// tensor cores:
+//   V_j[k] = sum_r in[j + r S] W_N^(j r) W_64^(r k),   out[j + k S] = V_j[k],
+// one product D = F' X per tile of 128 consecutive sub-transforms j (one
+// row).  X row n = j - j0, columns K = r (Re) and 64 + r (Im) of the
+// twiddled inputs, split into three bf16 parts; D lane 2k + c (Re / Im of
+// output k), column n.  Both sides move whole 1 KiB runs: a warp loads 32
+// consecutive j of one r, and each thread pair stores 32 consecutive j of one
+// k.  The epilogue can also write |V|^2 and the row maximum (the bucket
+// cutoff's samples).  F' stays in shared memory (one bulk copy per CTA).
+__global__ void __launch_bounds__(T64_THREADS, 1) tc64_last_pass_kernel(TcPassArgs a) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  unsigned char *A = tsm;                // 3 parts of F'
+  unsigned char *X = tsm + 3 * A_BYTES;  // 3 parts of the operand
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tsm + 3 * A_BYTES + 3 * X_BYTES);
+  unsigned long long *fbar = bar + 1;
+  unsigned *tmem_slot = reinterpret_cast<unsigned *>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float2 *__restrict__ in = reinterpret_cast<const float2 *>(a.in);
+  float2 *__restrict__ out = reinterpret_cast<float2 *>(a.out);
+  float *__restrict__ smp = reinterpret_cast<float *>(a.samples);
+  const float2 *__restrict__ thi = reinterpret_cast<const float2 *>(a.tw_hi);
+  const float2 *__restrict__ tlo = reinterpret_cast<const float2 *>(a.tw_lo);
+  const int logS = a.logN - 6;
+  const long long tpr = 1LL << (logS - 7);  // tiles per row
+  const long long ntiles = a.total >> 7;
+  const int th = a.tw_h;
+  const long long hmask = (1LL << th) - 1;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                 "r"(TP_N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(fbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(fbar)),
+                 "r"(3 * A_BYTES)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(A)),
+        "l"(a.F), "r"(3 * A_BYTES), "r"(smem_addr(fbar))
+        : "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const unsigned tmem = *tmem_slot;
+  const int quad = warp & 3, half = warp >> 2;
+  const unsigned tq = tmem + ((unsigned)(32 * quad) << 16);
+  const int L = 32 * quad + lane;
+  const int kc = L >> 1, c = L & 1;
+  unsigned phase = 0;
+  bool ok = true, f_ready = false;
+
+  for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const long long row = t / tpr, j0 = (t % tpr) << 7;
+    const float2 *src = in + row * a.bstride + j0;
+    // ---- operand: items (n, g), r = 8 g + q; a warp covers 32 consecutive n.
+    // All 32 loads of a thread's four items are issued before any is used.
+    const int n = tid & 127, gb = tid >> 7;  // items (n, gb + 2 it), it < 4
+    float2 xv[4][8];
+#pragma unroll
+    for (int it = 0; it < 4; it++)
+#pragma unroll
+      for (int q = 0; q < 8; q++) xv[it][q] = src[n + ((long long)(8 * (gb + 2 * it) + q) << logS)];
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+      const int g = gb + 2 * it;
+      const long long jn = j0 + n;
+      float re[8], im[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        float2 v = xv[it][q];
+        if (a.inverse) v.y = -v.y;
+        const long long mm = jn * (8 * g + q);  // < N
+        const float2 w = cmul(__ldg(&thi[mm >> th]), __ldg(&tlo[mm & hmask]));
+        v = cmul(v, w);
+        re[q] = v.x;
+        im[q] = v.y;
+      }
+      store_parts8_row(X, n, 8 * g, re);
+      store_parts8_row(X, n, 64 + 8 * g, im);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      bool go = true;
+      if (!f_ready) {
+        go = mbar_wait_bounded(smem_addr(fbar), 0);
+        f_ready = go;
+      }
+      if (go) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        constexpr unsigned IDESC = idesc_bf16(TC_M, TP_N);
+        const int pa[6] = {1, 0, 2, 0, 1, 0};
+        const int pb[6] = {1, 2, 0, 1, 0, 0};
+        for (int u = 0; u < 6; u++) {
+          const unsigned abase = smem_addr(A + pa[u] * A_BYTES);
+          const unsigned bbase = smem_addr(X + pb[u] * X_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < TC_K / 16; kk++) {
+            const unsigned long long ad = smem_desc(abase + kk * 256, 128, (TC_K / 8) * 128);
+            const unsigned long long bd = smem_desc(bbase + kk * 256, 128, (TC_K / 8) * 128);
+            const unsigned acc = (u > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{ .reg .pred p; setp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+                : "memory");
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_addr(bar))
+                     : "memory");
+      } else {
+        // nothing issued: arrive on the barrier so that every thread leaves its wait
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+        ok = false;
+        if (a.err) atomicExch(a.err, 1);
+      }
+    }
+    if (!mbar_wait_bounded(smem_addr(bar), phase)) {
+      ok = false;
+      if (tid == 0 && a.err) atomicExch(a.err, 1);
+    }
+    ok = __syncthreads_and(ok) != 0;  // warp-collective TMEM loads below: all or none
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) break;
+    // ---- outputs: this warp reads columns [64 half, 64 half + 64) of its
+    // lanes; thread c stores the 32 columns 64 half + 32 c .. of output kc
+    float tmax = 0.f;
+#pragma unroll 1
+    for (int hh = 0; hh < 32; hh += 16) {
+      unsigned ya[16], yb[16];
+      tmem_ld16_nowait(tq + (unsigned)(64 * half + hh), ya);
+      tmem_ld16_nowait(tq + (unsigned)(64 * half + 32 + hh), yb);
+      tmem_wait_ld();
+      const long long off = row * a.bstride + j0 + 64 * half + 32 * c + hh + ((long long)kc << logS);
+#pragma unroll
+      for (int i2 = 0; i2 < 16; i2 += 2) {
+        float re[2], im[2];
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const float send = __uint_as_float(c ? ya[i2 + e] : yb[i2 + e]);
+          const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+          const float own = __uint_as_float(c ? yb[i2 + e] : ya[i2 + e]);
+          re[e] = c ? recv : own;
+          im[e] = c ? own : recv;
+          if (a.inverse) im[e] = -im[e];
+        }
+        if (a.write_complex)
+          *reinterpret_cast<float4 *>(out + off + i2) = make_float4(re[0], im[0], re[1], im[1]);
+        if (smp) {
+          const float s0 = sq_sum_f(re[0], im[0]), s1 = sq_sum_f(re[1], im[1]);
+          *reinterpret_cast<float2 *>(smp + off + i2) = make_float2(s0, s1);
+          tmax = fmaxf(tmax, fmaxf(s0, s1));
+        }
+      }
+    }
+    if (smp && a.row_max) {
+      unsigned kmax = __float_as_uint(tmax);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned y = __shfl_down_sync(0xffffffffu, kmax, o);
+        kmax = y > kmax ? y : kmax;
+      }
+      if (lane == 0) atomicMax(reinterpret_cast<unsigned *>(a.row_max) + row, kmax);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // the operand buffer and TMEM are rewritten by the next tile
+  }
+  if (tid == 0 && !f_ready) (void)mbar_wait_bounded(smem_addr(fbar), 0);
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP_N) : "memory");
+}
+
 }  // namespace
 
 int launch_tc_dft64(const void *x, void *y, int nvec, int *err, cudaStream_t st) {
@@ -680,6 +891,42 @@ int launch_bounded_wait_probe(long long limit, int *gave_up, cudaStream_t st) {
 int tc_build_F(void **F) {
   GS_CUDA(cudaMalloc(F, 3 * FT_PART_BYTES));
   tc_build_F_kernel<<<(TC_M * (TC_K / 2) + 255) / 256, 256>>>(static_cast<unsigned char *>(*F));
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+int tc_build_F_smem(void **F) {
+  GS_CUDA(cudaMalloc(F, 3 * A_BYTES));
+  tc_build_F_smem_kernel<<<(TC_M * TC_K + 255) / 256, 256>>>(static_cast<unsigned char *>(*F));
+  GS_LAUNCHED();
+  return GSFFT_OK;
+}
+
+int launch_tc64_last_pass(const TcPassArgs &a, cudaStream_t st) {
+  // the last pass (Ns = N / 64), at least 128 sub-transforms per row, the
+  // inter-pass twiddle tables of the pass, 16-byte aligned rows
+  if (a.logN < 13 || a.logNs != a.logN - 6 || !a.tw_hi || !a.tw_lo || !a.F || a.nsum > 1)
+    return GSFFT_ERR_UNSUPPORTED;
+  if ((reinterpret_cast<uintptr_t>(a.in) & 15) || (reinterpret_cast<uintptr_t>(a.out) & 15) ||
+      (reinterpret_cast<uintptr_t>(a.samples) & 7) || (a.bstride & 1) || (a.row_max && !a.samples))
+    return GSFFT_ERR_UNSUPPORTED;
+  static PerContext<int> attr;  // the kernel's dynamic shared memory limit, per context
+  GS_CHECK(attr.ensure_at_least(T64_SMEM, [](int v) {
+    if (cudaFuncSetAttribute(tc64_last_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, v) ==
+        cudaSuccess)
+      return (int)GSFFT_OK;
+    set_last_error("tc64_last_pass_kernel: %d bytes of shared memory refused: %s", v,
+                   cudaGetErrorString(cudaGetLastError()));
+    return (int)GSFFT_ERR_CUDA;
+  }));
+  int dev = 0, sms = 0;
+  GS_CUDA(cudaGetDevice(&dev));
+  GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const long long ntiles = a.total >> 7;
+  long long grid = ntiles < sms ? ntiles : sms;
+  if (a.max_ctas > 0 && grid > a.max_ctas) grid = a.max_ctas;
+  if (grid < 1) return GSFFT_OK;
+  tc64_last_pass_kernel<<<(int)grid, T64_THREADS, T64_SMEM, st>>>(a);
   GS_LAUNCHED();
   return GSFFT_OK;
 }

@@ -117,6 +117,7 @@ def lib():
         "gsfft_stage_name": ([i], C.c_char_p),
         "gsfft_fft": ([P, P, ll, i, i, i, P], i),
         "gsfft_fft_tc": ([P, P, ll, i, i, P], i),
+        "gsfft_fft_tc64": ([P, P, ll, i, i, P], i),
         "gsfft_check_bounded_wait": ([ll, P], i),
         "gsfft_cutoff": ([P, i, i, i, i, P, P], i),
         "gsfft_cutoff_noalloc": ([P, i, i, i, i, P, P], i),
@@ -192,6 +193,11 @@ def fft(d_in, d_out, n, batch=1, sign=-1, precision=FP64, stream=0):
 def fft_tc(d_in, d_out, n, batch=1, sign=-1, stream=0):
     """FP32 FFT with the tensor-core radix-4096 first pass (n = 2^17 .. 2^26)."""
     check(lib().gsfft_fft_tc(d_in, d_out, n, batch, sign, stream or None), "gsfft_fft_tc")
+
+
+def fft_tc64(d_in, d_out, n, batch=1, sign=-1, stream=0):
+    """FP32 FFT with the tensor-core radix-64 last pass (n = 2^13 .. 2^20)."""
+    check(lib().gsfft_fft_tc64(d_in, d_out, n, batch, sign, stream or None), "gsfft_fft_tc64")
 
 
 def cutoff(d_samples, size, num, batch, precision, d_out, stream=0):

@@ -289,6 +289,15 @@ int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sig
 int gsfft_fft_tc(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
                  void *stream);
 
+/* The other tensor-core FFT plan, used for the bucket FFT where B allows it:
+ * n_fft = 2^L points, 13 <= L <= 20, a CUDA-core first pass of radix
+ * 2^(L-6), then a radix-64 last pass as one tcgen05 product per 128
+ * sub-transforms (three-part bf16 splits, fp32 accumulation), whose loads and
+ * stores move whole 1 KiB runs.  Same arguments and conventions as
+ * gsfft_fft_tc. */
+int gsfft_fft_tc64(const void *d_in, void *d_out, long long n_fft, int batch, int sign,
+                   void *stream);
+
 /* Tensor-core building block of the mixed bucket FFT (the DFT stages that
  * replace cuFFT's B-point transform, innerLoop.cu:247-262): nvec independent
  * forward 64-point DFTs of {float, float} vectors (d_in, d_out: nvec * 64

@@ -82,3 +82,22 @@ def test_tc_fft_matches_numpy(G, torch_cuda, n, batch, sign):
     want = np.fft.fft(x64, axis=1) if sign < 0 else np.fft.ifft(x64, axis=1) * n
     err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
     assert err.max() < 2e-6, err.max()
+
+
+@pytest.mark.parametrize("n,batch,sign", [(1 << 17, 9, -1), (1 << 13, 3, -1), (1 << 20, 2, -1),
+                                          (1 << 18, 1, 1), (1 << 16, 400, -1)])
+def test_tc64_fft_matches_numpy(G, torch_cuda, n, batch, sign):
+    """The FP32 FFT whose radix-64 last pass runs on the tensor cores (the
+    bucket FFT's plan for B = 2^13 .. 2^20): 2^13 x 3 gives 3 tiles of 128
+    sub-transforms, 2^16 x 400 about 21 tiles per CTA."""
+    torch = torch_cuda
+    rng = np.random.default_rng(n + batch + 7)
+    x = (rng.normal(size=(batch, n)) + 1j * rng.normal(size=(batch, n))).astype(np.complex64)
+    d_x = torch.from_numpy(x).cuda()
+    d_y = torch.zeros_like(d_x)
+    G.fft_tc64(d_x.data_ptr(), d_y.data_ptr(), n, batch, sign)
+    got = d_y.cpu().numpy().astype(np.complex128)
+    x64 = x.astype(np.complex128)
+    want = np.fft.fft(x64, axis=1) if sign < 0 else np.fft.ifft(x64, axis=1) * n
+    err = np.linalg.norm(got - want, axis=1) / np.linalg.norm(want, axis=1)
+    assert err.max() < 2e-6, err.max()
