@@ -80,6 +80,12 @@ class ClockSampler:
         self.idx = gpu_index
         self.proc = None
         self.lines = []
+        self.first = 0  # index of the first sample of the timed region
+
+    def mark(self):
+        """The timed region starts now: later samples are the ones reported
+        (the one just before it too, when none arrives inside it)."""
+        self.first = max(0, len(self.lines) - 1)
 
     def start(self):
         try:
@@ -96,6 +102,13 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def wait_first(self, timeout=10.0):
+        """Block until nvidia-smi has printed its first sample, so that its
+        start-up is over before a timed region begins."""
+        t0 = time.perf_counter()
+        while self.proc and not self.lines and time.perf_counter() - t0 < timeout:
+            time.sleep(0.01)
+
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -106,7 +119,7 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[self.first:]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -301,8 +314,7 @@ def run_ours(args, cfg):
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
     pf_flag = {"auto": 0, "gather": gsfft.FLAG_FORCE_GATHER, "stream": gsfft.FLAG_FORCE_STREAM}[args.pf]
-    tc_flag = (gsfft.FLAG_TC_BUCKET_FFT if args.tc_bucket else 0) | \
-        (gsfft.FLAG_TC_RLFC_FFT if args.tc_rlfc else 0)
+    tc_flag = bucket_flag(gsfft, args) | (gsfft.FLAG_TC_RLFC_FFT if args.tc_rlfc else 0)
     plans = {"fp64": gsfft.Plan(p, gsfft.FP64, pf_flag),
              "mixed": gsfft.Plan(p, gsfft.MIXED, pf_flag | tc_flag)}
     for pl in plans.values():
@@ -322,11 +334,16 @@ def run_ours(args, cfg):
         second pass over the same steps and draws, with CUDA events recorded
         around every stage on the stream it runs on, gives the stage times."""
         pl, xx = plans[name], xin[name]
+        if sampler:
+            # sampling runs through the warm-up and the timed region; its
+            # start-up (process spawn, first query) stays outside the latter
+            sampler.start()
+            sampler.wait_first()
         for s in range(args.warmup):
             pl.run(xx.data_ptr(), *draws[s], stream=sh)
         barrier()
         if sampler:
-            sampler.start()
+            sampler.mark()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for s in range(args.steps):
@@ -510,14 +527,15 @@ def run_ours(args, cfg):
 
     launches = plans["mixed"].launches_per_run() * args.steps
     value = job_rate(ws, args.steps, ms32 * 1e-3)
+    tcf = plans["mixed"].tensor_core_ffts()  # which FFTs of the timed plan use the tensor cores
     fp64 = job_rate(ws, args.steps, ms64 * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": ("f32+bf16x3/f64-estimate (mixed)" if (args.tc_bucket or args.tc_rlfc)
+        "dtype": ("f32+bf16x3/f64-estimate (mixed)" if any(tcf.values())
                   else "f32/f64-estimate (mixed)"),
-        "tensor_core_ffts": {"bucket": bool(args.tc_bucket), "rlfc": bool(args.tc_rlfc)},
+        "tensor_core_ffts": tcf,
         "data": "synthetic",
         "config": workload_config(cfg, {"global_batch": ws, "filter_design_ms_untimed":
                                         round(filter_ms, 1)}),
@@ -548,6 +566,13 @@ def run_ours(args, cfg):
 # further configurations (not the headline line): noisy, batched, large-k
 # ----------------------------------------------------------------------------
 
+def bucket_flag(gsfft, args):
+    """--tc-bucket / --cc-bucket as plan flags (neither: the plan's own rule)."""
+    if args.tc_bucket is None:
+        return 0
+    return gsfft.FLAG_TC_BUCKET_FFT if args.tc_bucket else gsfft.FLAG_CC_BUCKET_FFT
+
+
 def _plan_for(gsfft, torch, p, prec, dev, flags=0, keep_filter=None):
     d_ft = torch.zeros(p.w, dtype=torch.complex128, device=dev)
     d_ff = torch.zeros(p.n, dtype=torch.complex128, device=dev)
@@ -561,7 +586,7 @@ def _plan_for(gsfft, torch, p, prec, dev, flags=0, keep_filter=None):
 
 
 def tune_batch(gsfft, torch, params, plans, filters, xs, drs, sh, timed, cache_path, steps,
-               stream_counts=(16, 32, 64, 128)):
+               stream_counts=(16, 32, 64, 128), flags=0):
     """Autotuned batch: plans grouped by (n, B, W_RLFC, loops, RLFC_loops),
     one gsfft_autotune_plan per group (on that group's first signal, results
     cached in cache_path), every plan re-created with its group's shapes;
@@ -574,14 +599,14 @@ def tune_batch(gsfft, torch, params, plans, filters, xs, drs, sh, timed, cache_p
     for key, members in groups.items():
         r = members[0]
         d_ft, d_ff = filters[r]
-        t, ms = gsfft.autotune_plan(params[r], gsfft.MIXED, 0, xs[r].data_ptr(), d_ft.data_ptr(),
+        t, ms = gsfft.autotune_plan(params[r], gsfft.MIXED, flags, xs[r].data_ptr(), d_ft.data_ptr(),
                                     d_ff.data_ptr(), *drs[r], reps=5, cache_path=cache_path,
                                     stream=sh)
         shapes[key] = t
     tuned = []
     for i, p in enumerate(params):
         t = shapes[(p.n, p.B, p.W_RLFC, p.loops, p.RLFC_loops)]
-        pl = gsfft.Plan(p, gsfft.MIXED, 0, tuning=t)
+        pl = gsfft.Plan(p, gsfft.MIXED, flags, tuning=t)
         pl.set_filter(filters[i][0].data_ptr(), filters[i][1].data_ptr(), sh)
         tuned.append(pl)
     tune_s = time.perf_counter() - t0
@@ -674,6 +699,7 @@ def run_configs(args):
                 "vs_full_fft": {kk: {"missed_result": v["missed_result"],
                                      "rel_l2": float(np.sqrt(v["mse_k"] / p.k))} for kk, v in ev.items()}}
     elif args.workload == "batched256":
+        bflags = bucket_flag(gsfft, args)
         rng = np.random.default_rng(2024)
         plans, xs, drs, qs, params, filters = [], [], [], [], [], []
         while len(plans) < 256:
@@ -684,7 +710,7 @@ def run_configs(args):
             if stt != 0:
                 continue  # the reference would assert: draw again
             try:
-                pl = _plan_for(gsfft, torch, p, gsfft.MIXED, dev,
+                pl = _plan_for(gsfft, torch, p, gsfft.MIXED, dev, flags=bflags,
                                keep_filter=filters if args.tune else None)
             except RuntimeError:
                 continue  # a window layout this engine rejects: draw again
@@ -726,12 +752,13 @@ def run_configs(args):
                 "streams_value": 256e3 / ms_b, "graph_value": (256e3 / ms_g) if ms_g else None,
                 "sequential_value": 256e3 / ms_s,
                 "ms_per_batch": ms_g if ms_g else ms_b, "signals_by_q": {str(q): qs.count(q) for q in range(18, 25)},
-                "persistent_voting": bool(args.persistent_tail)}
+                "persistent_voting": bool(args.persistent_tail),
+                "tensor_core_bucket_ffts": sum(pl.tensor_core_ffts()["bucket"] for pl in plans)}
         batch.close()
         if args.tune:
             cache = args.tune_cache or os.path.join(PKG, "build", "tuning.txt")
             tuned, best, per_count, det = tune_batch(gsfft, torch, params, plans, filters, xs, drs,
-                                                     sh, timed, cache, args.steps)
+                                                     sh, timed, cache, args.steps, flags=bflags)
             for pl in plans:
                 pl.close()
             plans = tuned
@@ -808,10 +835,10 @@ def main():
     ap.add_argument("--pf", default="auto", choices=["auto", "gather", "stream"],
                     help="perm+filter form (auto: by the plan's DRAM byte model)")
     ap.add_argument("--tc-bucket", dest="tc_bucket", action="store_true",
-                    help="mixed bucket FFT with tensor-core passes")
+                    help="mixed bucket FFT with tensor-core passes for every B they support")
     ap.add_argument("--cc-bucket", dest="tc_bucket", action="store_false",
                     help="mixed bucket FFT on CUDA cores only")
-    ap.set_defaults(tc_bucket=False)
+    ap.set_defaults(tc_bucket=None)  # the plan's own rule (tensor cores for 2^17 <= B <= 2^20)
     ap.add_argument("--tc-rlfc", dest="tc_rlfc", action="store_true",
                     help="mixed RLFC FFT with the tensor-core first pass")
     ap.add_argument("--cc-rlfc", dest="tc_rlfc", action="store_false",

@@ -373,6 +373,13 @@ int gsfft_plan_describe(gsfft_plan plan, int *streaming, int *row_groups) {
   return GSFFT_OK;
 }
 
+int gsfft_plan_tensor_core_ffts(gsfft_plan plan, int *bucket, int *rlfc) {
+  if (!plan || !bucket || !rlfc) return GSFFT_ERR_PARAM;
+  *bucket = plan->impl->tc_bucket ? 1 : 0;
+  *rlfc = plan->impl->tc_rlfc ? 1 : 0;
+  return GSFFT_OK;
+}
+
 int gsfft_fft(const void *d_in, void *d_out, long long n_fft, int batch, int sign, int precision,
               void *stream) {
   if (!d_in || !d_out || batch < 1 || (sign != 1 && sign != -1)) return GSFFT_ERR_PARAM;

@@ -178,10 +178,15 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   if (s == GSFFT_OK) {
     int t = GSFFT_ERR_UNSUPPORTED;
     // tensor-core bucket FFT: the radix-64 last pass where B allows it
-    // (2^13 .. 2^20), else the radix-4096 first pass
-    if (precision == GSFFT_MIXED && (flags & GSFFT_FLAG_TC_BUCKET_FFT)) {
+    // (2^13 .. 2^20), else the radix-4096 first pass.  By default MIXED
+    // plans take it for 2^17 <= B <= 2^20: on the n = 2^27, k = 16000 step it
+    // measured 0.5007 against 0.5124 ms, while the batch of small signals
+    // (smaller B, one tile per CTA) ran slower with it.
+    const bool tc_asked = (flags & GSFFT_FLAG_TC_BUCKET_FFT) != 0;
+    const bool tc_default = !(flags & GSFFT_FLAG_CC_BUCKET_FFT) && p.B >= (1 << 17) && p.B <= (1 << 20);
+    if (precision == GSFFT_MIXED && (tc_asked || tc_default)) {
       t = fft_plan_init_tc64(P->fftB, p.B, p.loops);
-      if (t == GSFFT_ERR_UNSUPPORTED) t = fft_plan_init_tc(P->fftB, p.B, p.loops);
+      if (t == GSFFT_ERR_UNSUPPORTED && tc_asked) t = fft_plan_init_tc(P->fftB, p.B, p.loops);
     }
     P->tc_bucket = t == GSFFT_OK;
     if (!P->tc_bucket) s = fft_plan_init(P->fftB, p.B, precision, p.loops, tn.bucket_first_radix);
@@ -210,7 +215,9 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   if (s == GSFFT_OK &&
       (cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking) != cudaSuccess ||
        cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-       cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess)) {
+       cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&P->ev_bins, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&P->ev_rsel, cudaEventDisableTiming) != cudaSuccess)) {
     set_last_error("plan init: %s", cudaGetErrorString(cudaGetLastError()));
     s = GSFFT_ERR_CUDA;
   }
@@ -244,6 +251,8 @@ void plan_destroy(Plan *P) {
   for (cudaEvent_t e : P->events) cudaEventDestroy(e);
   if (P->ev_fork) cudaEventDestroy(P->ev_fork);
   if (P->ev_join) cudaEventDestroy(P->ev_join);
+  if (P->ev_bins) cudaEventDestroy(P->ev_bins);
+  if (P->ev_rsel) cudaEventDestroy(P->ev_rsel);
   if (P->side) cudaStreamDestroy(P->side);
   fft_plan_free(P->fftB);
   fft_plan_free(P->fftW);
@@ -363,10 +372,14 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
 
   // A6: bucket FFT of every loop, cutoff of the location loops.  They need
   // only the perm+filter, so they run on the plan's side stream beside A4's
-  // RLFC chain and join the main stream before the voting.
+  // RLFC chain.  The location loops' rows go first: the cutoff needs only
+  // them, and the main stream waits for the cutoff before the voting.  The
+  // estimation loops' rows follow on the side stream, beside the voting; the
+  // main stream waits for them before the estimation.
   GS_CUDA(cudaEventRecord(P->ev_fork, st));
   GS_CUDA(cudaStreamWaitEvent(P->side, P->ev_fork, 0));
   BEGIN_ON(ST_BUCKET_FFT, P->side);
+  const void *bsrc = P->bins;
   {
     FftIo io;
     io.samples = P->bsamp;
@@ -383,7 +396,8 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
       else
         src = P->bpart;
     }
-    GS_CHECK(fft_exec(P->fftB, src, P->bins, p.loops, -1, io, P->side));
+    GS_CHECK(fft_exec(P->fftB, src, P->bins, p.loops_loc, -1, io, P->side));
+    bsrc = src;
   }
   END_ON(ST_BUCKET_FFT, P->side);
   BEGIN_ON(ST_CUTOFF, P->side);
@@ -415,6 +429,20 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   GS_CHECK(select_top(P->rsamp, kb, p.W_RLFC, nullptr, p.B_thresh, p.RLFC_loops, p.W_RLFC, P->J2b,
                       p.B_thresh, nullptr, P->selW, st, rmax_w, P->floor_rel));
   END(ST_RLFC_SELECT);
+
+  // the estimation loops' bucket FFT (side stream), queued behind the RLFC
+  // cutoff: that cutoff is a cooperative launch whose whole grid must be
+  // resident, so the FFT's blocks would hold back its start
+  GS_CUDA(cudaEventRecord(P->ev_rsel, st));
+  GS_CUDA(cudaStreamWaitEvent(P->side, P->ev_rsel, 0));
+  if (p.loops > p.loops_loc) {
+    FftIo io;  // complex bins only: the estimation reads no samples
+    io.err = &P->ctl->err;
+    const size_t off = (size_t)(P->precision == GSFFT_FP64 ? 16 : 8) * p.loops_loc * p.B;
+    GS_CHECK(fft_exec(P->fftB, (const char *)bsrc + off, (char *)P->bins + off, p.loops - p.loops_loc, -1,
+                      io, P->side));
+  }
+  GS_CUDA(cudaEventRecord(P->ev_bins, P->side));
   BEGIN(ST_J2);
   // F_l needs only the set of J2 ids, not the sorted list; the sorted J2
   // (num_RLFC ids) is compacted on demand by plan_debug
@@ -438,7 +466,8 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   }  // voting
 
   if (phases & PH_EST) {
-  // A8: estimation; A9: k largest
+  // A8: estimation (after the estimation loops' bucket FFT); A9: k largest
+  GS_CUDA(cudaStreamWaitEvent(st, P->ev_bins, 0));
   BEGIN(ST_ESTIMATE);
   // the grid covers 8k candidates at one per thread (about 4.8k at the
   // 2^27 / 16000 workload); more are taken by the grid-stride loop

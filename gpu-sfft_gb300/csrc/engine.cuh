@@ -54,6 +54,8 @@ struct Plan {
   // side stream of the bucket FFT and cutoff (they need only the perm+filter)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_bins = nullptr;  // the estimation loops' bucket FFT is done
+  cudaEvent_t ev_rsel = nullptr;  // the RLFC cutoff has been queued on the main stream
   bool timing = false;
   std::vector<cudaEvent_t> events;  // 2 * ST_COUNT per recorded run (begin, end)
   int timed_runs = 0;

@@ -26,6 +26,7 @@ FLAG_FORCE_GATHER = 4
 FLAG_FORCE_STREAM = 8
 FLAG_TC_BUCKET_FFT = 16
 FLAG_TC_RLFC_FFT = 32
+FLAG_CC_BUCKET_FFT = 64
 SELECTION_FLOOR = 1e-10
 OK, ERR_PARAM, ERR_CAPACITY, ERR_ALLOC, ERR_CUDA, ERR_UNSUPPORTED, ERR_STATE, ERR_TIMEOUT = range(8)
 
@@ -98,6 +99,7 @@ def lib():
         "gsfft_debug_stages": ([P, P, C.POINTER(i), P, P, P], i),
         "gsfft_plan_launches_per_run": ([P], i),
         "gsfft_plan_describe": ([P, C.POINTER(i), C.POINTER(i)], i),
+        "gsfft_plan_tensor_core_ffts": ([P, C.POINTER(i), C.POINTER(i)], i),
         "gsfft_batch_create": ([C.POINTER(P), i, i, C.POINTER(P)], i),
         "gsfft_batch_destroy": ([P], i),
         "gsfft_run_batched": ([P, C.POINTER(P), P, P, P, P], i),
@@ -439,3 +441,10 @@ class Plan:
         st, g = C.c_int(0), C.c_int(0)
         check(lib().gsfft_plan_describe(self.h, C.byref(st), C.byref(g)), "gsfft_plan_describe")
         return {"streaming": bool(st.value), "row_groups": g.value}
+
+    def tensor_core_ffts(self):
+        """{'bucket': bool, 'rlfc': bool} -- which FFTs have a tensor-core pass."""
+        b, r = C.c_int(0), C.c_int(0)
+        check(lib().gsfft_plan_tensor_core_ffts(self.h, C.byref(b), C.byref(r)),
+              "gsfft_plan_tensor_core_ffts")
+        return {"bucket": bool(b.value), "rlfc": bool(r.value)}

@@ -65,14 +65,20 @@ typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
    would move fewer DRAM bytes */
 #define GSFFT_FLAG_FORCE_STREAM 8u   /* perm+filter (and the RLFC sub-sampling) by
    one ordered pass over the signal whenever the sizes allow it */
-#define GSFFT_FLAG_TC_BUCKET_FFT 16u /* MIXED: the B-point bucket FFT as a
-   radix-2^(L-12) pass and a 4096-point four-step pass whose two DFT_64 stages
-   run on the tensor cores (tcgen05, three-part bf16 split products
-   accumulated in fp32), when B = 2^L with 17 <= L <= 26 */
+#define GSFFT_FLAG_TC_BUCKET_FFT 16u /* MIXED: the B-point bucket FFT with a
+   tensor-core pass (tcgen05, three-part bf16 split products accumulated in
+   fp32) for any B it supports: a CUDA-core radix-2^(L-6) pass and a radix-64
+   last pass on the tensor cores when B = 2^L with 13 <= L <= 20, else a
+   4096-point four-step first pass on the tensor cores and a radix-2^(L-12)
+   pass when 17 <= L <= 26.  Without this flag or GSFFT_FLAG_CC_BUCKET_FFT,
+   MIXED plans take the radix-64 tensor-core form when 2^17 <= B <= 2^20
+   (measured faster on the n = 2^27, k = 16000 step; slower for the smaller
+   B of batched small signals) and CUDA-core passes otherwise. */
 #define GSFFT_FLAG_TC_RLFC_FFT 32u   /* MIXED: the same tensor-core radix-4096 first
    pass for the W_RLFC-point RLFC FFT, when W_RLFC = 2^L with 17 <= L <= 26 and
    the plan uses the streaming perm+filter (which writes the sub-samples the
    transform reads) */
+#define GSFFT_FLAG_CC_BUCKET_FFT 64u /* MIXED: the bucket FFT on CUDA cores only */
 
 /* Run parameters derived exactly as experiment.c:71-84 and
  * cuExperiment.cu:279-284 derive them. */
@@ -191,6 +197,10 @@ int gsfft_plan_launches_per_run(gsfft_plan plan);
  * streams the whole signal once (with *row_groups partial bin sets), 0 when
  * it gathers the loops*w tapped samples. */
 int gsfft_plan_describe(gsfft_plan plan, int *streaming, int *row_groups);
+
+/* Which FFTs of the plan have a tensor-core pass: *bucket and *rlfc set to 1
+ * or 0. */
+int gsfft_plan_tensor_core_ffts(gsfft_plan plan, int *bucket, int *rlfc);
 
 /* ---- batches --------------------------------------------------------- */
 

@@ -22,8 +22,10 @@ def test_tc_dft64_matches_numpy(G, torch_cuda, nvec):
 
 
 def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
-    """Mixed engine with the tensor-core bucket FFT (B = 2^17 = 32 x 4096)
-    against the CUDA-core mixed engine and the FP64 engine, same draws."""
+    """Mixed engine with the tensor-core bucket FFT (B = 2^17: the plan's
+    default for 2^17 <= B <= 2^20, and what GSFFT_FLAG_TC_BUCKET_FFT asks for)
+    against the CUDA-core mixed engine (GSFFT_FLAG_CC_BUCKET_FFT) and the FP64
+    engine, same draws."""
     from gsfft import synth
     torch = torch_cuda
     cfg = (24, 1600, 4.0, 2, 2, 5, 64, 2)
@@ -37,9 +39,12 @@ def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
     d32 = d64.to(torch.complex64)
     draws = synth.draws(5, p.n, p.W_RLFC, p.RLFC_loops, p.loops)
     res = {}
-    for name, prec, flags, xx in [("fp64", G.FP64, 0, d64), ("mixed", G.MIXED, 0, d32),
-                                  ("tc", G.MIXED, G.FLAG_TC_BUCKET_FFT, d32)]:
+    for name, prec, flags, xx in [("fp64", G.FP64, 0, d64), ("mixed", G.MIXED, G.FLAG_CC_BUCKET_FFT, d32),
+                                  ("tc", G.MIXED, G.FLAG_TC_BUCKET_FFT, d32),
+                                  ("default", G.MIXED, 0, d32)]:
         plan = G.Plan(p, prec, flags)
+        tcf = plan.tensor_core_ffts()
+        assert tcf["bucket"] == (name in ("tc", "default")) and not tcf["rlfc"]
         plan.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
         plan.run(xx.data_ptr(), *draws)
         r = plan.results()
@@ -49,6 +54,7 @@ def test_tc_bucket_fft_pipeline(G, O, torch_cuda):
         plan.close()
         res[name] = r
     assert res["tc"]["launches"] == res["mixed"]["launches"]  # two bucket-FFT passes either way
+    assert res["default"]["topk"].tobytes() == res["tc"]["topk"].tobytes()
     b_tc = res["tc"]["bins"].astype(np.complex128)
     b_cc = res["mixed"]["bins"].astype(np.complex128)
     assert np.linalg.norm(b_tc - b_cc) / np.linalg.norm(b_cc) < 1e-5
