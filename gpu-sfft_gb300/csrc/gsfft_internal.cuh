@@ -201,13 +201,15 @@ struct FftPlan {
   void *tw_lo[3] = {nullptr, nullptr, nullptr};
   int tw_h[3] = {0, 0, 0};
   void *tw_R[3] = {nullptr, nullptr, nullptr};  // exp(-2 pi i m / R) for the pass radix
-  bool tc[3] = {false, false, false};  // pass runs on the tensor cores (radix 4096, FP32)
-  void *tc_F = nullptr;                // DFT_64 operand of the tensor-core passes
+  bool tc[3] = {false, false, false};  // pass runs on the tensor cores (radix 4096 or 64, FP32)
+  void *tc_F = nullptr;                // DFT_64 operand of the tensor-core pass (its layout
+                                       // follows the pass: tc_build_F / tc_build_F_smem)
   void *scratch = nullptr; // one transform-sized buffer per batch entry (multi-pass)
   long long scratch_elems = 0;
 };
 
-// One radix-4096 pass of an FP32 FFT on the tensor cores (tc_dft.cu).
+// One tensor-core pass of an FP32 FFT (tc_dft.cu): the radix-4096 first
+// pass or the radix-64 last pass.
 struct TcPassArgs {
   const void *in;       // float2
   void *out;            // float2
@@ -224,7 +226,6 @@ struct TcPassArgs {
   int *err;             // set when a completion wait timed out (may be null)
   int nsum = 1;         // radix-4096 form: add nsum partial inputs sstride apart
   long long sstride = 0;
-  int max_ctas = 0;     // grid cap (0: one CTA per SM)
 };
 int tc_build_F(void **F);
 // radix 64 as the last pass (one DFT_64 product per 128 sub-transforms)

@@ -1,4 +1,8 @@
-// 64-point complex DFTs on the 5th-generation tensor cores (tcgen05).
+// 64-point complex DFTs on the 5th-generation tensor cores (tcgen05): a
+// building block over independent vectors (tc_dft64_kernel) and two FFT
+// passes built from it -- a radix-4096 first pass (two DFT_64 stages, a
+// warp-specialised two-tile pipeline) and a radix-64 last pass (one DFT_64
+// stage per 128 sub-transforms, coalesced both ways).
 //
 // A batch of length-64 complex vectors is transformed as one real matrix
 // product D = F * X: F is the 128 x 128 real form of the DFT matrix
@@ -923,8 +927,7 @@ int launch_tc64_last_pass(const TcPassArgs &a, cudaStream_t st) {
   GS_CUDA(cudaGetDevice(&dev));
   GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const long long ntiles = a.total >> 7;
-  long long grid = ntiles < sms ? ntiles : sms;
-  if (a.max_ctas > 0 && grid > a.max_ctas) grid = a.max_ctas;
+  const long long grid = ntiles < sms ? ntiles : sms;
   if (grid < 1) return GSFFT_OK;
   tc64_last_pass_kernel<<<(int)grid, T64_THREADS, T64_SMEM, st>>>(a);
   GS_LAUNCHED();
