@@ -667,7 +667,7 @@ int gsfft_stage_estimate(int precision, const int *d_cand, int num, const void *
   double *mag2 = nullptr;
   RunCtl *ctl = nullptr;
   int s = GSFFT_OK;
-  if (cudaMalloc(&hinv, sizeof(double2) * (nb + 1)) != cudaSuccess ||
+  if (cudaMalloc(&hinv, hinv_bytes(nb)) != cudaSuccess ||
       cudaMalloc(&mag2, sizeof(double) * num) != cudaSuccess ||
       cudaMalloc(&ctl, sizeof(RunCtl)) != cudaSuccess)
     s = GSFFT_ERR_ALLOC;

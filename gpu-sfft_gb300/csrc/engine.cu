@@ -58,7 +58,9 @@ __global__ void store_draws_kernel(Draws d, Draws *out) {
   if (threadIdx.x == 0) *out = d;
 }
 
-// hinv[idx] = conj(H)/|H|^2 with H = filter_freq[(n - d) mod n], d = idx - nb/2
+// hinv[idx] = conj(H)/|H|^2 with H = filter_freq[(n - d) mod n], d = idx - nb/2,
+// followed by the same nb + 1 values rounded to float (the mixed estimate's
+// ranking table)
 __global__ void hinv_kernel(const double2 *__restrict__ ff, int n, int nb, double2 *hinv) {
   const int idx = blockIdx.x * 256 + threadIdx.x;
   if (idx > nb) return;
@@ -66,7 +68,9 @@ __global__ void hinv_kernel(const double2 *__restrict__ ff, int n, int nb, doubl
   const int dist = (int)(((long long)n - d) & (long long)(n - 1));
   const double2 H = ff[dist];
   const double a2 = __dadd_rn(__dmul_rn(H.x, H.x), __dmul_rn(H.y, H.y));
-  hinv[idx] = make_double2(H.x / a2, -H.y / a2);
+  const double2 v = make_double2(H.x / a2, -H.y / a2);
+  hinv[idx] = v;
+  reinterpret_cast<float2 *>(hinv + nb + 1)[idx] = make_float2((float)v.x, (float)v.y);
 }
 
 template <typename P> int alloc(P **p, size_t bytes) {
@@ -123,7 +127,7 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
 #define A(ptr, bytes) \
   if (s == GSFFT_OK) s = alloc(&P->ptr, (bytes))
   A(filt, V * p.w);
-  A(hinv, sizeof(double2) * (nb + 1));
+  A(hinv, hinv_bytes(nb));
   A(rsamp, T * (size_t)p.RLFC_loops * p.W_RLFC);
   A(J2b, sizeof(int) * (size_t)p.RLFC_loops * p.B_thresh);
   A(J2, sizeof(int) * (size_t)p.RLFC_loops * p.B_thresh);

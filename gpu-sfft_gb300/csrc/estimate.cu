@@ -9,9 +9,10 @@
 //   v_j = bins_j[h] * conj(H[(n - d) mod n]) / |H[(n - d) mod n]|^2
 // The reciprocal response conj(H)/|H|^2 is precomputed in FP64 for the n/B + 1
 // offsets d the formula can produce, so the estimate is one complex multiply
-// in FP64 per loop (bins are promoted from FP32 in the mixed path).  The
-// median of the real parts and of the imaginary parts is taken separately,
-// element (loops-1)/2 of the ascending order (:855-861).
+// in FP64 per loop.  The median of the real parts and of the imaginary parts
+// is taken separately, element (loops-1)/2 of the ascending order
+// (:855-861).  In the mixed path (FP32 bins) the ranking runs in FP32 and only
+// the two median estimates are computed in FP64 (estimate_dev.cuh).
 #include "estimate_dev.cuh"
 
 namespace gsfft {

@@ -86,6 +86,9 @@ int vote_block_ints(int B_thresh);
 // A8: estimates + |value|^2 keys for the candidates.
 // cap: candidate capacity; the grid is sized for `expect` candidates (a
 // grid-stride loop covers up to cap)
+// bytes of the reciprocal filter-response table: nb + 1 double2, then the
+// same values as float2 (hinv_kernel writes both)
+inline size_t hinv_bytes(int nb) { return (sizeof(double2) + sizeof(float2)) * (size_t)(nb + 1); }
 int launch_estimate(int precision, const int *cand, const RunCtl *ctl, int cap, int expect,
                     const void *bins, int loops, int n, int B, const Draws &d,
                     const double2 *hinv, DevNode *nodes, double *mag2, cudaStream_t st);

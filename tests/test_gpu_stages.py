@@ -159,8 +159,15 @@ def test_estimate(G, O, torch_cuda, prec):
     got = d_out.cpu().numpy().view(G.NODE)
     np.testing.assert_array_equal(got["key"], ref["key"])
     scale = np.abs(ref["x"] + 1j * ref["y"]).max()
-    assert np.abs(got["x"] - ref["x"]).max() <= 1e-13 * scale
-    assert np.abs(got["y"] - ref["y"]).max() <= 1e-13 * scale
+    # FP64: every estimate and the median ranking in FP64.  Mixed: the median
+    # loops are ranked in FP32 and only the chosen estimates computed in FP64,
+    # so two estimates closer than FP32 rounding may swap: at most that far off.
+    tol = 1e-13 if prec == 0 else 1e-6
+    assert np.abs(got["x"] - ref["x"]).max() <= tol * scale
+    assert np.abs(got["y"] - ref["y"]).max() <= tol * scale
+    if prec == 1:
+        # and nearly always exactly the FP64 median
+        assert (np.abs(got["x"] - ref["x"]) <= 1e-13 * scale).mean() > 0.99
 
 
 @pytest.mark.parametrize("prec", [0, 1])
