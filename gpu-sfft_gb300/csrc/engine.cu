@@ -483,7 +483,9 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
 
   if (phases & PH_TOPK) {
   BEGIN(ST_TOPK);
-  GS_CHECK(select_top(P->mag2, 8, P->cap, &P->ctl->cand_count, p.k, 1, P->cap, P->topk_idx, p.k,
+  // k largest |estimate|^2: 8-byte keys (FP64 path) or 4-byte keys (mixed path)
+  GS_CHECK(select_top(P->mag2, P->precision == GSFFT_FP64 ? 8 : 4, P->cap, &P->ctl->cand_count, p.k, 1,
+                      P->cap, P->topk_idx, p.k,
                       &P->ctl->n_topk, P->selK, st));
   GS_CHECK(launch_gather_nodes(P->nodes, P->topk_idx, &P->ctl->n_topk, p.k, P->topk, st));
   END(ST_TOPK);

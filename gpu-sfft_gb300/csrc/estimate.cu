@@ -13,6 +13,8 @@
 // is taken separately, element (loops-1)/2 of the ascending order
 // (:855-861).  In the mixed path (FP32 bins) the ranking runs in FP32 and only
 // the two median estimates are computed in FP64 (estimate_dev.cuh).
+// mag2 receives the top-k keys |estimate|^2: doubles in the FP64 path, floats
+// (in the same buffer) in the mixed path, whose top-k selects on 4-byte keys.
 #include "estimate_dev.cuh"
 
 namespace gsfft {
@@ -64,7 +66,12 @@ estimate_kernel(const int *__restrict__ cand, const RunCtl *ctl, int cap,
   nd.x = re;
   nd.y = im;
   nodes[i] = nd;
-  mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+  if constexpr (sizeof(T) == 4) {
+    const float fre = (float)re, fim = (float)im;  // the mixed path's 4-byte top-k key
+    reinterpret_cast<float *>(mag2)[i] = __fadd_rn(__fmul_rn(fre, fre), __fmul_rn(fim, fim));
+  } else {
+    mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+  }
 }
 
 __global__ void gather_nodes_kernel(const DevNode *__restrict__ nodes, const int *__restrict__ idx,

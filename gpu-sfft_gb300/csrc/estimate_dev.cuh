@@ -143,7 +143,9 @@ __device__ __forceinline__ void estimate_block(const int *__restrict__ cand, con
       nd.x = re;
       nd.y = im;
       nodes[i] = nd;
-      mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+      // the top-k key: |estimate|^2 in FP32 (the mixed path selects on 4-byte keys)
+      const float fre = (float)re, fim = (float)im;
+      reinterpret_cast<float *>(mag2)[i] = __fadd_rn(__fmul_rn(fre, fre), __fmul_rn(fim, fim));
     }
     return;
   }
