@@ -52,6 +52,7 @@ struct TailPlan {
   RunCtl *ctl;
   const Draws *draws;
   int vote_blocks;         // blocks of each stage (B_thresh / 8 buckets, one a warp)
+  int packed;              // vote table of 2-bit counters
   int per_item;            // consecutive blocks of a stage per work item
 };
 
@@ -124,6 +125,7 @@ batch_tail_kernel(const TailPlan *__restrict__ plans, const TailRange *__restric
     w.bm = tp.bm_sig + (size_t)(tp.W / 32) * l;
     w.fmax = &tp.ctl->fmax[l];
     w.a = (unsigned)tp.draws->a[l];
+    w.packed = tp.packed;
     const unsigned epoch = *tp.epoch;
     const int nblk = tp.vote_blocks;
     int *blk_pre = tp.blk + nblk + 1;
@@ -200,6 +202,7 @@ int batch_tail_create(Plan *const *plans, int count, BatchTail **out) {
     t.ctl = P->ctl;
     t.draws = P->d_draws;
     t.vote_blocks = (p.B_thresh + WPB - 1) / WPB;
+    t.packed = P->packed_vote ? 1 : 0;
     t.per_item = kBlocksPerItem;
     max_stages = std::max(max_stages, stages_of(p));
   }

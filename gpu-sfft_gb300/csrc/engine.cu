@@ -13,7 +13,9 @@
 //   bsamp        loops x B T                      |bins|^2
 //   J            loops_loc x B_thresh int         heavy buckets per location loop
 //   bm_j2, bm_sig  W/32 and loops_loc x W/32 u32  residue bitmaps
-//   vote         n u32                            epoch << 8 | count
+//   vote         n u32                            epoch << 8 | count, or (at most 3
+//                                                location loops) two n/16-word
+//                                                tables of 2-bit counters
 //   cand, nodes, mag2, topk_idx, topk             candidate list and results
 #include "engine.cuh"
 
@@ -179,6 +181,8 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
   }
 #undef A
   P->floor_rel = (flags & GSFFT_FLAG_RAW_SELECTION) ? 0.0 : 1e-10;
+  // 2-bit vote counters (n/4 bytes, L2-resident) when no count can pass 3
+  P->packed_vote = p.loops_loc <= 3;
   if (s == GSFFT_OK) {
     int t = GSFFT_ERR_UNSUPPORTED;
     // tensor-core bucket FFT: the radix-64 last pass where B allows it
@@ -221,7 +225,10 @@ int plan_create(const gsfft_params &pp, int precision, unsigned flags, int max_c
        cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming) != cudaSuccess ||
        cudaEventCreateWithFlags(&P->ev_bins, cudaEventDisableTiming) != cudaSuccess ||
-       cudaEventCreateWithFlags(&P->ev_rsel, cudaEventDisableTiming) != cudaSuccess)) {
+       cudaEventCreateWithFlags(&P->ev_rsel, cudaEventDisableTiming) != cudaSuccess ||
+       cudaStreamCreateWithFlags(&P->aux, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&P->ev_vclr, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&P->ev_voted, cudaEventDisableTiming) != cudaSuccess)) {
     set_last_error("plan init: %s", cudaGetErrorString(cudaGetLastError()));
     s = GSFFT_ERR_CUDA;
   }
@@ -257,6 +264,9 @@ void plan_destroy(Plan *P) {
   if (P->ev_join) cudaEventDestroy(P->ev_join);
   if (P->ev_bins) cudaEventDestroy(P->ev_bins);
   if (P->ev_rsel) cudaEventDestroy(P->ev_rsel);
+  if (P->ev_vclr) cudaEventDestroy(P->ev_vclr);
+  if (P->ev_voted) cudaEventDestroy(P->ev_voted);
+  if (P->aux) cudaStreamDestroy(P->aux);
   if (P->side) cudaStreamDestroy(P->side);
   fft_plan_free(P->fftB);
   fft_plan_free(P->fftW);
@@ -264,6 +274,23 @@ void plan_destroy(Plan *P) {
   select_scratch_free(P->selW);
   select_scratch_free(P->selK);
   delete P;
+}
+
+// Clears the packed vote table the next run uses: table ((epoch + 1) & 1) of
+// the two n/16-word tables, epoch being this run's (advanced by its first kernel).
+__global__ void vote_clear_kernel(unsigned *vote, unsigned words, const unsigned *epoch) {
+  uint4 *t = reinterpret_cast<uint4 *>(vote + (((*epoch + 1u) & 1u) ? words : 0u));
+  const unsigned n4 = words / 4;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x)
+    t[i] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+int launch_vote_clear(unsigned *vote, int n, const unsigned *d_epoch, cudaStream_t st) {
+  const unsigned words = (unsigned)n / 16;
+  const unsigned blocks = std::min(608u, (words / 4 + 255) / 256);
+  vote_clear_kernel<<<blocks, 256, 0, st>>>(vote, words, d_epoch);
+  GS_LAUNCHED();
+  return GSFFT_OK;
 }
 
 int launch_hinv(const double2 *d_ff, int n, int nb, double2 *hinv, cudaStream_t st) {
@@ -382,6 +409,7 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   // main stream waits for them before the estimation.
   GS_CUDA(cudaEventRecord(P->ev_fork, st));
   GS_CUDA(cudaStreamWaitEvent(P->side, P->ev_fork, 0));
+
   BEGIN_ON(ST_BUCKET_FFT, P->side);
   const void *bsrc = P->bins;
   {
@@ -454,8 +482,14 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
                                     P->bm_sig, P->ctl, st));
   END(ST_J2);
 
-  // the side stream joins back before the voting
+  // the side stream joins back before the voting, and the voting waits for
+  // the clear of its packed table, queued by the previous eager run.  A clear
+  // recorded in a captured graph is a graph node that every replay runs before
+  // it completes (and an event recorded in a capture cannot be waited on
+  // outside it); a capture needs no wait either, its replays following one
+  // another on a stream.
   GS_CUDA(cudaStreamWaitEvent(st, P->ev_join, 0));
+  if (P->packed_vote && !capturing && P->vclr_eager) GS_CUDA(cudaStreamWaitEvent(st, P->ev_vclr, 0));
   }  // front
 
   if (phases & PH_VOTE) {
@@ -465,11 +499,21 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
   for (int l = 0; l < p.loops_loc; l++)
     GS_CHECK(launch_vote_loop(l, P->J + (size_t)l * p.B_thresh, p.B_thresh, p.n, p.B, p.W_RLFC,
                               P->bm_sig + wW * l, d, p.loops_thresh, P->d_epoch, P->vote, P->cand,
-                              P->cap, P->cnt, P->blk, P->ctl, l + 1 >= p.loops_thresh, st));
+                              P->cap, P->cnt, P->blk, P->ctl, l + 1 >= p.loops_thresh, st,
+                              P->packed_vote));
   END(ST_VOTE);
   }  // voting
 
   if (phases & PH_EST) {
+  if (P->packed_vote) {
+    // the voting is done: clear the other packed table for the next run,
+    // beside this run's estimation and top-k
+    GS_CUDA(cudaEventRecord(P->ev_voted, st));
+    GS_CUDA(cudaStreamWaitEvent(P->aux, P->ev_voted, 0));
+    GS_CHECK(launch_vote_clear(P->vote, p.n, P->d_epoch, P->aux));
+    GS_CUDA(cudaEventRecord(P->ev_vclr, P->aux));
+    P->vclr_eager = !capturing;
+  }
   // A8: estimation (after the estimation loops' bucket FFT); A9: k largest
   GS_CUDA(cudaStreamWaitEvent(st, P->ev_bins, 0));
   BEGIN(ST_ESTIMATE);
@@ -489,6 +533,9 @@ int plan_run(Plan *P, const void *d_x, const int *offs, const int *a, const int 
                       &P->ctl->n_topk, P->selK, st));
   GS_CHECK(launch_gather_nodes(P->nodes, P->topk_idx, &P->ctl->n_topk, p.k, P->topk, st));
   END(ST_TOPK);
+  // the clear of the next run's vote table (queued after the voting) joins the
+  // run here; it has long finished beside the estimation and top-k
+  if (P->packed_vote && (phases & PH_EST)) GS_CUDA(cudaStreamWaitEvent(st, P->ev_vclr, 0));
   }  // top-k
 #undef BEGIN
 #undef END

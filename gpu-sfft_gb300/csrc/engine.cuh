@@ -31,7 +31,8 @@ struct Plan {
   void *bins = nullptr, *bsamp = nullptr;
   int *J = nullptr;
   unsigned *bm_j2 = nullptr, *bm_sig = nullptr, *tile_tmp = nullptr;
-  unsigned *vote = nullptr;
+  unsigned *vote = nullptr;  // n epoch-tagged entries, or n/16 words of 2-bit counters
+  bool packed_vote = false;  // 2-bit counters (at most 3 location loops)
   int *cand = nullptr, *cnt = nullptr, *blk = nullptr;
   DevNode *nodes = nullptr;
   double *mag2 = nullptr;
@@ -56,6 +57,10 @@ struct Plan {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev_bins = nullptr;  // the estimation loops' bucket FFT is done
   cudaEvent_t ev_rsel = nullptr;  // the RLFC cutoff has been queued on the main stream
+  cudaStream_t aux = nullptr;     // clears the packed vote table beside the FFTs
+  cudaEvent_t ev_vclr = nullptr;  // the next run's packed vote table is clear
+  bool vclr_eager = false;        // ev_vclr last recorded by an eager run (not in a capture)
+  cudaEvent_t ev_voted = nullptr; // this run's voting is done
   bool timing = false;
   std::vector<cudaEvent_t> events;  // 2 * ST_COUNT per recorded run (begin, end)
   int timed_runs = 0;
@@ -87,6 +92,7 @@ const char *stage_name(int i);
 int plan_debug(Plan *P, int *h_J2, int *num_RLFC, int *h_J, void *h_bins, cudaStream_t st);
 
 int launch_hinv(const double2 *d_ff, int n, int nb, double2 *hinv, cudaStream_t st);
+int launch_vote_clear(unsigned *vote, int n, const unsigned *d_epoch, cudaStream_t st);
 int launch_convert_taps(const double2 *d_ft, void *dst, int w, bool to_float, cudaStream_t st);
 
 // persistent tail of a batch (batch_tail.cu): the voting of every plan in

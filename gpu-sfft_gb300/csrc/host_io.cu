@@ -86,11 +86,13 @@ __global__ void energy_partial_kernel(const double2 *__restrict__ xf, long long 
 }
 
 // One block: top-k hits, the top-k correction of the energy, and the
-// candidate hits read from the epoch-tagged vote table.
+// candidate hits read from the vote table (epoch-tagged entries, or 2-bit
+// counters when packed).
 __global__ void evaluate_kernel(const DevNode *__restrict__ topk, const int *n_topk,
                                 const int *__restrict__ tloc, int k_true, const double2 *__restrict__ xf,
                                 const unsigned *__restrict__ vote, unsigned epoch, unsigned thresh,
-                                const double *part, int nparts, double *out /* err, found_est, found_res */) {
+                                int packed /* n when packed, else 0 */, const double *part, int nparts,
+                                double *out /* err, found_est, found_res */) {
   __shared__ double sd[1024];
   __shared__ int si[1024], sr[1024];
   const int t = threadIdx.x;
@@ -114,8 +116,15 @@ __global__ void evaluate_kernel(const DevNode *__restrict__ topk, const int *n_t
   }
   int found_est = 0;
   for (int i = t; i < k_true; i += 1024) {
-    const unsigned v = vote[tloc[i]];
-    found_est += ((v >> 8) == epoch && (v & 255u) >= thresh) ? 1 : 0;
+    const unsigned loc = (unsigned)tloc[i];
+    if (packed) {
+      // this run's table of the two (epoch & 1)
+      const unsigned *tab = vote + ((epoch & 1u) ? ((unsigned)packed >> 4) : 0u);
+      found_est += ((tab[loc >> 4] >> (2 * (loc & 15u))) & 3u) >= thresh ? 1 : 0;
+    } else {
+      const unsigned v = vote[loc];
+      found_est += ((v >> 8) == epoch && (v & 255u) >= thresh) ? 1 : 0;
+    }
   }
   sd[t] = e;
   si[t] = found_est;
@@ -185,7 +194,8 @@ int plan_evaluate(Plan *P, const complex_t *d_xf, const int *d_true_loc, int k_t
   if (s == GSFFT_OK) {
     evaluate_kernel<<<1, 1024, 0, st>>>(P->topk, &P->ctl->n_topk, d_true_loc, k_true,
                                         (const double2 *)d_xf, P->vote, P->epoch,
-                                        (unsigned)P->p.loops_thresh, buf, parts, buf + parts);
+                                        (unsigned)P->p.loops_thresh, P->packed_vote ? P->p.n : 0, buf,
+                                        parts, buf + parts);
     if (cudaGetLastError() != cudaSuccess) s = GSFFT_ERR_CUDA;
   }
   double h[3] = {0, 0, 0};

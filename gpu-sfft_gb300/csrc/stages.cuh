@@ -79,7 +79,7 @@ int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, co
 int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
                      const unsigned *bitmap_l, const Draws &d, int loops_thresh, const unsigned *epoch,
                      unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
-                     bool may_complete, cudaStream_t st);
+                     bool may_complete, cudaStream_t st, bool packed = false);
 // ints needed by the blk scratch of launch_vote_loop
 int vote_block_ints(int B_thresh);
 

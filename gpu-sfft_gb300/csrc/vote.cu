@@ -189,7 +189,7 @@ int launch_sigma_from_blocks(const int *J2b, int total, int W, int loops_loc, co
 int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
                      const unsigned *bitmap_l, const Draws &d, int loops_thresh, const unsigned *epoch,
                      unsigned *vote, int *cand, int cap, int *cnt, int *blk, RunCtl *ctl,
-                     bool may_complete, cudaStream_t st) {
+                     bool may_complete, cudaStream_t st, bool packed) {
   WalkArgs w;
   w.J = J;
   w.Bt = B_thresh;
@@ -199,6 +199,7 @@ int launch_vote_loop(int l, const int *J, int B_thresh, int n, int B, int W,
   w.bm = bitmap_l;
   w.fmax = &ctl->fmax[l];
   w.a = (unsigned)d.a[l];
+  w.packed = packed ? 1 : 0;
   const int grid = (B_thresh + WPB - 1) / WPB;
   if (!may_complete) {
     GS_CUDA(launch_pdl(vote_mark_kernel, dim3(grid), dim3(VT), 0, st, w, epoch, vote));

@@ -55,7 +55,57 @@ struct WalkArgs {
   const unsigned *bm;
   const int *fmax;
   unsigned a;
+  int packed;  // vote tables of 2-bit counters (16 per word; two tables used on alternate
+               // runs) instead of epoch-tagged 32-bit entries
 };
+
+// The vote table.  Epoch-tagged: entry = epoch << 8 | count, never cleared
+// between runs, read and written plainly (a location is visited at most once
+// per pass).  Packed (at most 3 location loops, so counts fit 2 bits): 16
+// counters per word, n / 4 bytes -- small enough to stay in L2 -- updated
+// with word atomics, since neighbouring locations share a word.  There are
+// two packed tables, the run with epoch e using table e & 1; after a run's
+// voting the other one is cleared for the next run (vote_clear_kernel), so
+// the clear overlaps the run's latency-bound tail.
+__device__ __forceinline__ unsigned *packed_table(const WalkArgs &w, unsigned *vote, unsigned epoch) {
+  return vote + ((epoch & 1u) ? ((unsigned)w.n >> 4) : 0u);
+}
+// vote_update: the votes of up to four visited locations, independent so
+// that their table accesses overlap; cnt[q] = the count after the vote.
+__device__ __forceinline__ void vote_update(const WalkArgs &w, unsigned epoch, unsigned *vote,
+                                            const unsigned (&loc)[4], int nq, unsigned (&cnt)[4]) {
+  if (w.packed) {
+    unsigned *tab = packed_table(w, vote, epoch);
+    unsigned old[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (q < nq) old[q] = atomicAdd(&tab[loc[q] >> 4], 1u << (2 * (loc[q] & 15u)));
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (q < nq) cnt[q] = ((old[q] >> (2 * (loc[q] & 15u))) & 3u) + 1u;
+    return;
+  }
+  unsigned e[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    if (q < nq) e[q] = __ldcg(&vote[loc[q]]);
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    if (q < nq) {
+      const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
+      vote[loc[q]] = (epoch << 8) | cv;
+      cnt[q] = cv;
+    }
+}
+// whether location loc's count is exactly the threshold (after a pass's votes)
+__device__ __forceinline__ bool vote_at_threshold(const WalkArgs &w, unsigned epoch, const unsigned *vote,
+                                                  unsigned loc, unsigned thresh) {
+  if (w.packed) {
+    const unsigned *tab = vote + ((epoch & 1u) ? ((unsigned)w.n >> 4) : 0u);
+    return ((__ldcg(&tab[loc >> 4]) >> (2 * (loc & 15u))) & 3u) == thresh;
+  }
+  return __ldcg(&vote[loc]) == ((epoch << 8) | thresh);
+}
 
 // low = ceil((J - 0.5) * n/B) reduced mod n (innerLoop.cu:792), in integers.
 __device__ __forceinline__ int window_low(int J, int n, int nb) {
@@ -141,7 +191,7 @@ __device__ __forceinline__ unsigned count_walk(const WalkArgs &w, int t, unsigne
     // independent, so they overlap instead of paying one DRAM latency each
     unsigned app = 0;  // bits of this lane's mask whose count reached the threshold
     while (mask) {
-      unsigned loc[4], e[4];
+      unsigned loc[4];
       int nq = 0;
       const unsigned before = mask;
 #pragma unroll
@@ -153,18 +203,12 @@ __device__ __forceinline__ unsigned count_walk(const WalkArgs &w, int t, unsigne
           nq = q + 1;
         }
       }
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (q < nq) e[q] = __ldcg(&vote[loc[q]]);
+      unsigned cv[4];
+      vote_update(w, epoch, vote, loc, nq, cv);
       unsigned hitq = 0;  // bit q: position q of this round reached the threshold
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        if (q < nq) {
-          const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
-          vote[loc[q]] = (epoch << 8) | cv;
-          hitq |= (unsigned)(cv == thresh) << q;
-        }
-      }
+      for (int q = 0; q < 4; q++)
+        if (q < nq) hitq |= (unsigned)(cv[q] == thresh) << q;
       // the round's positions are the lowest set bits of `before`, in order
       unsigned taken = before & ~mask;
 #pragma unroll
@@ -208,7 +252,6 @@ __device__ __forceinline__ void write_bucket(const WalkArgs &w, int t, unsigned 
     return;
   }
   const unsigned nmask = (unsigned)w.n - 1u;
-  const unsigned want = (epoch << 8) | thresh;
   for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
     // appended positions of this lane, in bit order
     unsigned app = 0;
@@ -227,7 +270,7 @@ __device__ __forceinline__ void write_bucket(const WalkArgs &w, int t, unsigned 
       }
 #pragma unroll
       for (int q = 0; q < 4; q++)
-        if (q < nq && __ldcg(&vote[loc[q]]) == want) app |= 1u << bit[q];
+        if (q < nq && vote_at_threshold(w, epoch, vote, loc[q], thresh)) app |= 1u << bit[q];
     }
     unsigned ctot;
     long long o = next + warp_excl_scan((unsigned)__popc(app), &ctot);
@@ -299,7 +342,7 @@ __device__ __forceinline__ void vote_mark_block(const WalkArgs &w, unsigned epoc
   const unsigned nmask = (unsigned)w.n - 1u;
   for_each_chunk(w, w.J[t], [&](unsigned mask, const ChunkPos &pos) {
     while (mask) {
-      unsigned loc[4], e[4];
+      unsigned loc[4], cv[4];
       int nq = 0;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
@@ -310,15 +353,7 @@ __device__ __forceinline__ void vote_mark_block(const WalkArgs &w, unsigned epoc
           nq = q + 1;
         }
       }
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (q < nq) e[q] = __ldcg(&vote[loc[q]]);
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-        if (q < nq) {
-          const unsigned cv = ((e[q] >> 8) == epoch) ? (e[q] & 255u) + 1u : 1u;
-          vote[loc[q]] = (epoch << 8) | cv;
-        }
+      vote_update(w, epoch, vote, loc, nq, cv);
     }
   });
 }
