@@ -470,12 +470,20 @@ def run_ours(args, cfg):
     pipe = None
     if args.in_flight > 1:
         P = args.in_flight
-        pplans, pxs = [plans["mixed"]], [x32]
+        # With several signals in flight the CUDA-core bucket FFT is the
+        # faster choice (the tensor-core pass's one-tile CTAs hold whole SMs
+        # that the other signals' kernels could use): 2311 against 2233
+        # sparse FFTs/s with eight in flight, same box.  An explicit
+        # --tc-bucket / --cc-bucket applies as given.
+        pflags = pf_flag | (tc_flag if args.tc_bucket is not None
+                            else gsfft.FLAG_CC_BUCKET_FFT | (tc_flag & ~gsfft.FLAG_TC_BUCKET_FFT))
+        pplans, pxs = [], [x32]
         for i in range(1, P):
             xi, _, _, _ = synth.signal_torch(n, k, seed=100 * (rank + 1) + i, device=dev)
             pxs.append(xi.to(torch.complex64))
             del xi
-            pl = gsfft.Plan(p, gsfft.MIXED, pf_flag | tc_flag)
+        for i in range(P):
+            pl = gsfft.Plan(p, gsfft.MIXED, pflags)
             pl.set_filter(d_ft.data_ptr(), d_ff.data_ptr(), sh)
             pplans.append(pl)
         batch = gsfft.Batch(pplans, streams=P)
@@ -494,9 +502,10 @@ def run_ours(args, cfg):
         pms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
         pipe = {"signals_in_flight": P, "streams": P,
                 "value": job_rate(ws, args.steps * P, pms * 1e-3), "unit": UNIT,
-                "ms_per_sfft": pms / (args.steps * P)}
+                "ms_per_sfft": pms / (args.steps * P),
+                "tensor_core_ffts": pplans[0].tensor_core_ffts()}
         batch.close()
-        for pl in pplans[1:]:
+        for pl in pplans:
             pl.close()
         del pxs
 
