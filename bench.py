@@ -791,8 +791,11 @@ def run_configs(args):
         d_ft = torch.zeros(p.w, dtype=torch.complex128, device=dev)
         d_ff = torch.zeros(p.n, dtype=torch.complex128, device=dev)
         gsfft.design_filter(p, d_ft.data_ptr(), d_ff.data_ptr())
+        # eight concurrent plans: the CUDA-core bucket FFT unless a form is given
+        # (see the signals-in-flight figure of the headline workload)
+        lflags = bucket_flag(gsfft, args) if args.tc_bucket is not None else gsfft.FLAG_CC_BUCKET_FFT
         for i in range(8):
-            pl = gsfft.Plan(p, gsfft.MIXED, 0)
+            pl = gsfft.Plan(p, gsfft.MIXED, lflags)
             pl.set_filter(d_ft.data_ptr(), d_ff.data_ptr())
             x64, loc, coef, X = synth.signal_torch(p.n, p.k, seed=50 + i, snr_db=30.0, device=dev)
             xs.append(x64.to(torch.complex64))
