@@ -73,7 +73,9 @@ typedef enum { GSFFT_FP64 = 0, GSFFT_MIXED = 1 } gsfft_precision;
    pass when 17 <= L <= 26.  Without this flag or GSFFT_FLAG_CC_BUCKET_FFT,
    MIXED plans take the radix-64 tensor-core form when 2^17 <= B <= 2^20
    (measured faster on the n = 2^27, k = 16000 step; slower for the smaller
-   B of batched small signals) and CUDA-core passes otherwise. */
+   B of batched small signals) and CUDA-core passes otherwise.  Plans that
+   run concurrently (several signals in flight) do better with
+   GSFFT_FLAG_CC_BUCKET_FFT. */
 #define GSFFT_FLAG_TC_RLFC_FFT 32u   /* MIXED: the same tensor-core radix-4096 first
    pass for the W_RLFC-point RLFC FFT, when W_RLFC = 2^L with 17 <= L <= 26 and
    the plan uses the streaming perm+filter (which writes the sub-samples the
