@@ -12,6 +12,9 @@ CFGS = {  # (q, k, Bcst, loops_loc, loops_thresh, loops_est, RLFC_cst, RLFC_loop
     "n14": (14, 10, 2.5, 2, 2, 5, 16, 2),
     "n16": (16, 20, 1.0, 2, 2, 5, 8, 2),
     "n18_3loc": (18, 100, 1.0, 3, 2, 6, 32, 2),
+    # three location loops, all three needed: vote counts reach 3 (the packed
+    # tables' 2-bit maximum)
+    "n18_3thr": (18, 100, 1.0, 3, 3, 6, 32, 2),
     "config1": (20, 1000, 1.40, 2, 2, 5, 128, 2),
 }
 
