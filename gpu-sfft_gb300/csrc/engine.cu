@@ -36,11 +36,10 @@ __global__ void convert_taps_kernel(const double2 *__restrict__ src, void *dst, 
   else reinterpret_cast<double2 *>(dst)[i] = v;
 }
 
-// First kernel of every run: clears the run state and the row maxima and
-// advances the device epoch (a graph replay of the run advances it too).
 // First kernel of a run (launched normally, after everything before it):
-// block 0 clears the control block and the row maxima and advances the epoch;
-// every block zeroes part of the residue bitmaps F_l.
+// block 0 clears the control block and the row maxima and advances the device
+// epoch (a graph replay of the run advances it too); every block zeroes part
+// of the residue bitmaps F_l.
 __global__ void run_begin_kernel(RunCtl *ctl, unsigned long long *rmax, int nrmax, unsigned *epoch,
                                  unsigned *bm, long long bm_words) {
   pdl_enter();
