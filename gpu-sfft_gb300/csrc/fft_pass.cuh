@@ -129,14 +129,15 @@ template <typename T> __host__ __device__ constexpr int minb_of(int logr) {
 __host__ __device__ constexpr int padded(int i) { return i + (i >> 4); }
 // Row stride in elements.  Rows start in different banks; when a warp's load
 // or store phase interleaves G rows (FP32, 2 <= G <= 16, each row handled by
-// whole warps in the butterfly stages), a pitch of 32/G 8-byte elements past
-// a multiple of 16 makes the G x (32/G) lanes fill every bank pair exactly
-// twice (two wavefronts) instead of colliding.
+// whole warps in the butterfly stages), a pitch of 16/G 8-byte elements past
+// a multiple of 16 puts the G rows' runs of consecutive elements on disjoint
+// bank pairs within each half-warp (16 lanes x 8 bytes = one wavefront), and
+// fills every bank pair exactly twice over the whole warp.
 template <typename T> __host__ __device__ constexpr int rowpitch(int logr) {
   return padded(1 << logr) +
          ((sizeof(T) == 4 && g_of<T>(logr) >= 2 && g_of<T>(logr) <= 16 &&
            nt_of<T>(logr) / g_of<T>(logr) >= 32)
-              ? 32 / g_of<T>(logr)
+              ? 16 / g_of<T>(logr)
               : 1);
 }
 // twiddle table exp(-2 pi i m / R) copied into shared memory when it fits
@@ -199,6 +200,37 @@ __device__ __forceinline__ void apply_pretw(V (&v)[Q][E], const PreTw &pt, int g
   }
 }
 
+// Twiddles of one radix-E butterfly of a Stockham stage: v[e] *= twR[k e step]
+// (twR[m] = exp(-2 pi i m / R)).
+template <typename V, int E>
+__device__ __forceinline__ void stage_twiddles(V (&v)[E], const V *__restrict__ twR, int k, int step) {
+  if constexpr (sizeof(v[0].x) == 8 || E < 4) {
+    // FP64: exact table entries (its FP64 pipe, not shared memory, is the limit)
+#pragma unroll
+    for (int e = 1; e < E; e++) v[e] = cmul(v[e], twR[k * e * step]);
+  } else {
+    // FP32: two table reads (w, w^4), other powers by products at most four
+    // deep -- the strided table reads were the shared-memory bank hot spot
+    V w[E];
+    w[1] = twR[k * step];
+    w[2] = cmul(w[1], w[1]);
+    w[3] = cmul(w[2], w[1]);
+    w[4] = twR[4 * k * step];
+#pragma unroll
+    for (int e = 5; e < 8 && e < E; e++) w[e] = cmul(w[4], w[e - 4]);
+    if constexpr (E == 16) {
+      w[8] = cmul(w[4], w[4]);
+#pragma unroll
+      for (int e = 9; e < 12; e++) w[e] = cmul(w[8], w[e - 8]);
+      w[12] = cmul(w[8], w[4]);
+#pragma unroll
+      for (int e = 13; e < 16; e++) w[e] = cmul(w[12], w[e - 12]);
+    }
+#pragma unroll
+    for (int e = 1; e < E; e++) v[e] = cmul(v[e], w[e]);
+  }
+}
+
 // One Stockham stage of radix E inside shared memory, for all G rows, after
 // stages whose radices multiply to Ns = 2^LOGNS.  All strides are compile-time
 // constants: with padded(i) = i + i/16, NB = R/E and t < NB,
@@ -239,34 +271,7 @@ __device__ __forceinline__ void smem_stage(V *sm, const V *__restrict__ twR, con
 #pragma unroll
       for (int e = 0; e < E; e++) v[q][e] = rp[e * NB + ((e * NB) >> 4)];
     }
-    if constexpr (LOGNS > 0) {
-      const int k = t & (Ns - 1);
-      if constexpr (sizeof(v[0][0].x) == 8 || E < 4) {
-        // FP64: exact table entries (its FP64 pipe, not shared memory, is the limit)
-#pragma unroll
-        for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], twR[k * e * step]);
-      } else {
-        // FP32: two table reads (w, w^4), other powers by products at most four
-        // deep -- the strided table reads were the shared-memory bank hot spot
-        V w[E];
-        w[1] = twR[k * step];
-        w[2] = cmul(w[1], w[1]);
-        w[3] = cmul(w[2], w[1]);
-        w[4] = twR[4 * k * step];
-#pragma unroll
-        for (int e = 5; e < 8 && e < E; e++) w[e] = cmul(w[4], w[e - 4]);
-        if constexpr (E == 16) {
-          w[8] = cmul(w[4], w[4]);
-#pragma unroll
-          for (int e = 9; e < 12; e++) w[e] = cmul(w[8], w[e - 8]);
-          w[12] = cmul(w[8], w[4]);
-#pragma unroll
-          for (int e = 13; e < 16; e++) w[e] = cmul(w[12], w[e - 12]);
-        }
-#pragma unroll
-        for (int e = 1; e < E; e++) v[q][e] = cmul(v[q][e], w[e]);
-      }
-    }
+    if constexpr (LOGNS > 0) stage_twiddles<V, E>(v[q], twR, t & (Ns - 1), step);
     dft_reg<V, E>(v[q]);
   }
   __syncthreads();
@@ -428,6 +433,126 @@ __device__ __forceinline__ void row_max_update(void *rm, long long b, float v) {
   if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned *>(rm) + b, k);
 }
 
+// ---------------------------------------------------------------- fused I/O
+// FP32 radix 2^11 and 2^12 (G = 4 sub-transforms of one batch row per CTA,
+// plain loads): the first stage takes its inputs straight from global memory
+// into registers and the last stage stores its outputs straight to global
+// memory, so every element passes through shared memory twice (once per
+// inner stage boundary) instead of four times, and the load and store phases
+// with their barriers are gone.  In both fused stages the lanes take the G
+// sub-transforms fastest (g = tid % G): each warp load or store moves whole
+// 32-byte sectors (G consecutive sub-transforms are adjacent on input, and
+// on output once Ns >= G; with Ns = 1 each sub-transform's outputs are
+// contiguous and 8 lanes write 64 bytes of it).
+template <typename T> __host__ __device__ constexpr bool fused_io(int logr) {
+  return sizeof(T) == 4 && (logr == 11 || logr == 12);
+}
+
+// Radix of the first stage of a radix-2^LOGR transform (the remainder stage).
+template <int LOGR> __host__ __device__ constexpr int first_radix() {
+  return LOGR % 4 == 0 ? 16 : (1 << (LOGR % 4));
+}
+
+// First stage (Ns = 1, radix E = first_radix): butterfly t of row g reads
+// r = t + e NB, e < E, from src[r S] (src = the row's sub-transform j,
+// S = 2^logS), applies the conjugation and inter-pass twiddles in registers
+// and writes its outputs to shared memory.  Butterflies go to lanes so that
+// the shared-memory stores of each half-warp hit 16 distinct bank pairs with
+// the 16/G pitch: for E = 16 (padded(16 t + e) = 17 t + e) four consecutive t
+// per half-warp; for E = 8 (padded(8 t + e) = 8 t + t/2 + e) four t of one
+// parity, as consecutive t would put t and t + 2 on the same pair.
+template <typename V, int LOGR, int G>
+__device__ __forceinline__ void fused_first_stage(V *sm, const V *__restrict__ src, int logS, const PreTw &pt,
+                                                  int inverse) {
+  constexpr int R = 1 << LOGR, E = first_radix<LOGR>();
+  constexpr int LOGE = E == 2 ? 1 : (E == 4 ? 2 : (E == 8 ? 3 : 4));
+  constexpr int NT = nt_of<float>(LOGR), TPF = NT / G, RP = rowpitch<float>(LOGR);
+  constexpr int NB = R / E, Q = NB / TPF;
+  static_assert(G == 4 && E >= 8 && Q * TPF == NB, "fused first stage: G = 4, radix 8 or 16");
+  const int tid = threadIdx.x, g = tid % G;
+  int t0;
+  if constexpr (E == 8) {
+    const int tl = (tid >> 2) & 7;  // lane / G
+    t0 = (tid >> 5) * 8 + (((tl & 3) << 1) | (tl >> 2));
+  } else {
+    t0 = tid / G;
+  }
+  V v[Q][E];
+  const V *p = src + ((long long)t0 << logS);
+  const long long sq = (long long)TPF << logS, se = (long long)NB << logS;
+#pragma unroll
+  for (int q = 0; q < Q; q++)
+#pragma unroll
+    for (int e = 0; e < E; e++) v[q][e] = __ldg(p + q * sq + e * se);
+  if (pt.on) {
+    apply_pretw<V, E, Q, NB, TPF>(v, pt, g, t0);  // conjugates too when inverse
+  } else if (inverse) {
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+#pragma unroll
+      for (int e = 0; e < E; e++) v[q][e].y = -v[q][e].y;
+  }
+  V *s = sm + g * RP;
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    dft_reg<V, E>(v[q]);
+    // Stockham output of butterfly t (Ns = 1): positions t E + e, all in one
+    // run of 16 (padded adds (t E) / 16 to each)
+    V *wp = s + padded((t0 + q * TPF) << LOGE);
+#pragma unroll
+    for (int e = 0; e < E; e++) wp[e] = v[q][bitrev<E>(e)];
+  }
+}
+
+// Inner stages: radix 16 after Ns = 2^LOGNS, up to the last stage.
+template <typename V, int LOGR, int G, int LOGNS>
+__device__ __forceinline__ void fused_mid_stages(V *sm, const V *__restrict__ twR, const PreTw &pt) {
+  if constexpr (LOGNS + 4 < LOGR) {
+    smem_stage<V, LOGR, G, 16, LOGNS>(sm, twR, pt);
+    fused_mid_stages<V, LOGR, G, LOGNS + 4>(sm, twR, pt);
+  }
+}
+
+// Last stage (radix 16, Ns = R/16): butterfly t of row g reads t + e NB from
+// shared memory and gives X[t + e NB] of sub-transform j, stored at
+// d0 + (t + e NB) Ns_global (complex and / or |X|^2 with the row maximum).
+template <typename T, typename V, int LOGR, int G>
+__device__ __forceinline__ void fused_last_stage(const V *sm, const V *__restrict__ twR, const PassArgs &a,
+                                                 long long b, long long d0, int logNs) {
+  constexpr int R = 1 << LOGR, E = 16;
+  constexpr int NT = nt_of<T>(LOGR), TPF = NT / G, RP = rowpitch<T>(LOGR);
+  constexpr int NB = R / E, Q = NB / TPF;
+  static_assert(Q * TPF == NB, "fused last stage: whole butterflies per thread");
+  const int tid = threadIdx.x, g = tid % G, t0 = tid / G;
+  const V *s = sm + g * RP;
+  V *__restrict__ out = reinterpret_cast<V *>(a.out);
+  T *__restrict__ smp = reinterpret_cast<T *>(a.samples);
+  T tmax = 0;
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int t = t0 + q * TPF;
+    V v[E];
+    const V *rp = s + padded(t);
+#pragma unroll
+    for (int e = 0; e < E; e++) v[e] = rp[e * NB + ((e * NB) >> 4)];
+    stage_twiddles<V, E>(v, twR, t, 1);  // k = t mod Ns = t, step R / (Ns E) = 1
+    dft_reg<V, E>(v);
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      V x = v[bitrev<E>(e)];
+      if (a.inverse) x.y = -x.y;
+      const long long d = d0 + ((long long)(t + e * NB) << logNs);
+      if (a.write_complex) out[d] = x;
+      if (smp) {
+        const T sv = sq_sum(x);
+        smp[d] = sv;
+        tmax = sv > tmax ? sv : tmax;
+      }
+    }
+  }
+  if (smp && a.row_max) row_max_update(a.row_max, b, tmax);
+}
+
 template <typename T, int LOGR>
 __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_kernel(PassArgs a) {
   pdl_enter();
@@ -474,6 +599,20 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
   // the first stage keeps its inputs in registers without spilling)
   pt.on = LOGR >= 11 && LOGR <= 13 && sizeof(T) == 4 && g_fast_in && !gx && a.nsum <= 1 &&
           logNs > 0;
+  if constexpr (fused_io<T>(LOGR)) {
+    // S >= G with both powers of two: the grid covers the batch exactly and
+    // all G sub-transforms of a CTA lie in one batch row
+    if (g_fast_in && !gx && a.nsum <= 1) {
+      const long long u = u0 + tid % G;
+      const long long b = u >> logS, j = u & Smask;
+      fused_first_stage<V, LOGR, G>(sm, in + b * a.bstride + j, logS, pt, a.inverse);
+      __syncthreads();
+      fused_mid_stages<V, LOGR, G, (LOGR % 4 == 0 ? 4 : LOGR % 4)>(sm, twR, pt);
+      const long long d0 = b * a.bstride + ((j >> logNs) << (logNs + LOGR)) + (j & Nsmask);
+      fused_last_stage<T, V, LOGR, G>(sm, twR, a, b, d0, logNs);
+      return;
+    }
+  }
   if (g_fast_in && !gx) {
     const int g = tid % G, r0 = tid / G;
     const long long u = u0 + g;
