@@ -458,9 +458,10 @@ template <int LOGR> __host__ __device__ constexpr int first_radix() {
 // S = 2^logS), applies the conjugation and inter-pass twiddles in registers
 // and writes its outputs to shared memory.  Butterflies go to lanes so that
 // the shared-memory stores of each half-warp hit 16 distinct bank pairs with
-// the 16/G pitch: for E = 16 (padded(16 t + e) = 17 t + e) four consecutive t
-// per half-warp; for E = 8 (padded(8 t + e) = 8 t + t/2 + e) four t of one
-// parity, as consecutive t would put t and t + 2 on the same pair.
+// the 16/G pitch, i.e. the half-warp's four butterflies fall on four
+// consecutive pairs: for E = 16 (padded(16 t + e) = 17 t + e) four consecutive
+// t; for E = 8 (padded(8 t + e) = 8 t + t/2 + e) four t of one parity (with
+// consecutive t, t and t + 2 would share a pair).
 template <typename V, int LOGR, int G>
 __device__ __forceinline__ void fused_first_stage(V *sm, const V *__restrict__ src, int logS, const PreTw &pt,
                                                   int inverse) {
@@ -605,7 +606,9 @@ __global__ void __launch_bounds__(nt_of<T>(LOGR), minb_of<T>(LOGR)) fft_pass_ker
     if (g_fast_in && !gx && a.nsum <= 1) {
       const long long u = u0 + tid % G;
       const long long b = u >> logS, j = u & Smask;
-      fused_first_stage<V, LOGR, G>(sm, in + b * a.bstride + j, logS, pt, a.inverse);
+      PreTw ptf = pt;  // inter-pass twiddles in registers wherever Ns > 1
+      ptf.on = logNs > 0;
+      fused_first_stage<V, LOGR, G>(sm, in + b * a.bstride + j, logS, ptf, a.inverse);
       __syncthreads();
       fused_mid_stages<V, LOGR, G, (LOGR % 4 == 0 ? 4 : LOGR % 4)>(sm, twR, pt);
       const long long d0 = b * a.bstride + ((j >> logNs) << (logNs + LOGR)) + (j & Nsmask);
