@@ -13,7 +13,8 @@ def dev(torch, a):
 
 
 @pytest.mark.parametrize("n,batch", [(256, 3), (4096, 2), (8192, 1), (1 << 14, 2), (1 << 17, 3),
-                                     (1 << 20, 1), (1 << 22, 2), (1 << 25, 1)])
+                                     (1 << 20, 1), (1 << 22, 2), (1 << 23, 1), (1 << 24, 1),
+                                     (1 << 25, 1)])
 @pytest.mark.parametrize("prec", [0, 1])
 def test_fft_vs_numpy(G, torch_cuda, n, batch, prec):
     torch = torch_cuda
