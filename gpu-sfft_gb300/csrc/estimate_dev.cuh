@@ -147,34 +147,34 @@ __device__ __forceinline__ void estimate_block(const int *__restrict__ cand, con
       const float fre = (float)re, fim = (float)im;
       reinterpret_cast<float *>(mag2)[i] = __fadd_rn(__fmul_rn(fre, fre), __fmul_rn(fim, fim));
     }
-    return;
-  }
-  for (int i = bid * nt + threadIdx.x; i < count; i += nblk * nt) {
-    const unsigned loc = (unsigned)__ldcg(&cand[i]);
-    double vr[L], vi[L];
+  } else {
+    for (int i = bid * nt + threadIdx.x; i < count; i += nblk * nt) {
+      const unsigned loc = (unsigned)__ldcg(&cand[i]);
+      double vr[L], vi[L];
 #pragma unroll
-    for (int j = 0; j < L; j++) {
-      const unsigned p = ((unsigned)d.ai[j] * loc) & nmask;
-      int h = (int)(p >> lognb);
-      int dd = (int)(p & (unsigned)(nb - 1));
-      if (dd > nb / 2) {
-        h = (h + 1) & (B - 1);
-        dd -= nb;
+      for (int j = 0; j < L; j++) {
+        const unsigned p = ((unsigned)d.ai[j] * loc) & nmask;
+        int h = (int)(p >> lognb);
+        int dd = (int)(p & (unsigned)(nb - 1));
+        if (dd > nb / 2) {
+          h = (h + 1) & (B - 1);
+          dd -= nb;
+        }
+        const double2 H = __ldg(&hinv[dd + nb / 2]);
+        const typename Cx<T>::V bv = bins[(size_t)j * B + h];
+        const double bx = (double)bv.x, by = (double)bv.y;
+        vr[j] = fma(bx, H.x, -(by * H.y));
+        vi[j] = fma(bx, H.y, by * H.x);
       }
-      const double2 H = __ldg(&hinv[dd + nb / 2]);
-      const typename Cx<T>::V bv = bins[(size_t)j * B + h];
-      const double bx = (double)bv.x, by = (double)bv.y;
-      vr[j] = fma(bx, H.x, -(by * H.y));
-      vi[j] = fma(bx, H.y, by * H.x);
+      const double re = median_reg<L>(vr), im = median_reg<L>(vi);
+      DevNode nd;
+      nd.key = loc;
+      nd.pad = 0;
+      nd.x = re;
+      nd.y = im;
+      nodes[i] = nd;
+      mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
     }
-    const double re = median_reg<L>(vr), im = median_reg<L>(vi);
-    DevNode nd;
-    nd.key = loc;
-    nd.pad = 0;
-    nd.x = re;
-    nd.y = im;
-    nodes[i] = nd;
-    mag2[i] = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
   }
 }
 
