@@ -343,9 +343,10 @@ int gsfft_cutoff_floor(const void *d_samples, int size, int num, int batch, int 
  * without waiting; d_out is ready once the stream reaches that point.
  * The first call in each CUDA context (each device, and again after a
  * cudaDeviceReset) looks up the array's device address (and may load this
- * library's device code there), so make it before any stream capture starts.  Every call on a device shares the array: calls that may
- * overlap in time (other streams, unordered host threads) race and give
- * undefined results; calls ordered on one stream are safe. */
+ * library's device code there), so make it before any stream capture
+ * starts.  Every call on a device shares the array: calls that may overlap in
+ * time (other streams, unordered host threads) race and give undefined
+ * results; calls ordered on one stream are safe. */
 #define GSFFT_NOALLOC_MAX_SIZE (1 << 24)
 #define GSFFT_NOALLOC_MAX_BATCH 8
 int gsfft_cutoff_noalloc(const void *d_samples, int size, int num, int batch, int precision,

@@ -74,6 +74,47 @@ def test_cutoff_arguments_rejected(G):
     assert L.gsfft_cutoff(None, 100, 10, 1, G.FP64, fake, None) == G.ERR_PARAM
 
 
+def test_binding_constants_match_header(G):
+    """The Python binding's flags, status codes and limits are the header's."""
+    import re
+    text = open(G.HEADER).read()
+    defines = {m.group(1): m.group(2) for m in
+               re.finditer(r"#define (GSFFT_[A-Z0-9_]+) +(\(1 << \d+\)|\d+)u?", text)}
+
+    def val(name):
+        v = defines[name]
+        m = re.fullmatch(r"\(1 << (\d+)\)", v)
+        return 1 << int(m.group(1)) if m else int(v)
+
+    for flag in ("QUIRK_RESIDUE", "RAW_SELECTION", "FORCE_GATHER", "FORCE_STREAM",
+                 "TC_BUCKET_FFT", "TC_RLFC_FFT", "CC_BUCKET_FFT"):
+        assert getattr(G, "FLAG_" + flag) == val("GSFFT_FLAG_" + flag), flag
+    assert G.NOALLOC_MAX_SIZE == val("GSFFT_NOALLOC_MAX_SIZE")
+    assert G.NOALLOC_MAX_BATCH == val("GSFFT_NOALLOC_MAX_BATCH")
+    codes = dict(re.findall(r"\b(GSFFT_(?:OK|ERR_[A-Z]+)) = (\d+)", text))
+    for name in ("OK", "ERR_PARAM", "ERR_CAPACITY", "ERR_ALLOC", "ERR_CUDA", "ERR_UNSUPPORTED",
+                 "ERR_STATE", "ERR_TIMEOUT"):
+        assert getattr(G, name) == int(codes["GSFFT_" + name]), name
+
+
+def test_noalloc_cutoff_arguments_and_limits(G):
+    """The no-allocation cutoff checks its arguments like gsfft_cutoff and
+    rejects requests beyond its fixed scratch with GSFFT_ERR_CAPACITY, all
+    before any device work."""
+    L = G.lib()
+    fake = C.c_void_p(16)  # never dereferenced: every call below is rejected first
+    nc = L.gsfft_cutoff_noalloc
+    assert nc(fake, 100, 100, 1, G.FP64, fake, None) == G.ERR_PARAM   # num == size
+    assert nc(fake, 100, 0, 1, G.FP64, fake, None) == G.ERR_PARAM     # num < 1
+    assert nc(fake, 100, 10, 0, G.FP64, fake, None) == G.ERR_PARAM    # no rows
+    assert nc(fake, 100, 10, 1, 7, fake, None) == G.ERR_PARAM         # no such precision
+    assert nc(None, 100, 10, 1, G.FP64, fake, None) == G.ERR_PARAM
+    assert nc(fake, 100, 10, 1, G.FP64, None, None) == G.ERR_PARAM
+    assert nc(fake, G.NOALLOC_MAX_SIZE + 1, 10, 1, G.MIXED, fake, None) == G.ERR_CAPACITY
+    assert b"exceed" in L.gsfft_last_error()
+    assert nc(fake, 1000, 10, G.NOALLOC_MAX_BATCH + 1, G.FP64, fake, None) == G.ERR_CAPACITY
+
+
 @pytest.mark.parametrize("field,value,status", [
     ("n", 3000, "ERR_PARAM"),            # not a power of two
     ("B", 3000, "ERR_PARAM"),
