@@ -281,7 +281,6 @@ struct SelectScratch {
   int max_batch = 0, max_tiles = 0;
   bool single_launch = true;   // cluster / cooperative form allowed (else multi-launch)
 };
-extern bool g_select_coop;  // use the single-launch select (cluster or cooperative form)
 // Byte sizes of the SelectScratch regions for max_batch rows of at most
 // max_size samples (what select_scratch_init allocates); state and coop_hist
 // must hold zeros when a selection starts.

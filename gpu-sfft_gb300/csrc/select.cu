@@ -943,13 +943,11 @@ void select_scratch_free(SelectScratch &s) {
 
 size_t select_state_bytes() { return sizeof(SelState); }
 
-bool g_select_coop = true;  // single-launch select (cluster or cooperative) when the device supports it
-
 int select_top(const void *keys, int key_bytes, long long size, const int *size_dev, int num,
                int batch, long long row_stride, int *out, long long out_stride, int *count_out,
                SelectScratch &s, cudaStream_t st, const void *row_max, double floor_rel) {
   if (size_dev && batch != 1) return GSFFT_ERR_PARAM;
-  if (g_select_coop && s.single_launch && batch <= MAXB && batch <= s.max_batch &&
+  if (s.single_launch && batch <= MAXB && batch <= s.max_batch &&
       (size + SEL_TILE - 1) / SEL_TILE <= s.max_tiles) {
     for (const bool clu : {true, false}) {
       if (clu && !(size <= CLUSTER_ROW_MAX || size_dev)) continue;
