@@ -309,7 +309,7 @@ int gsfft_tc_dft64(const void *d_in, void *d_out, int nvec, void *stream) {
     s = GSFFT_ERR_CUDA;
   if (s == GSFFT_OK && herr) {
     set_last_error("gsfft_tc_dft64: a tensor-core completion wait timed out");
-    s = GSFFT_ERR_CUDA;
+    s = GSFFT_ERR_TIMEOUT;
   }
   cudaFree(err);
   return s;
@@ -465,7 +465,8 @@ int gsfft_fft_tc64(const void *d_in, void *d_out, long long n_fft, int batch, in
 
 int gsfft_cutoff(const void *d_samples, int size, int num, int batch, int precision, int *d_out,
                  void *stream) {
-  if (!d_samples || !d_out || size < 1 || num < 1 || num >= size || batch < 1)
+  if (!d_samples || !d_out || size < 1 || num < 1 || num >= size || batch < 1 ||
+      (precision != GSFFT_FP64 && precision != GSFFT_MIXED))
     return GSFFT_ERR_PARAM;
   SelectScratch ss;
   int s = select_scratch_init(ss, batch, size);
@@ -592,8 +593,8 @@ int gsfft_stage_perm_filter_stream(int precision, const void *d_x, int n,
   if (s == GSFFT_OK && cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     s = GSFFT_ERR_CUDA;
   if (s == GSFFT_OK && herr) {
-    set_last_error("a device-side wait timed out (streaming perm+filter)");
-    s = GSFFT_ERR_CUDA;
+    set_last_error("gsfft_stage_perm_filter_stream: a copy-completion wait timed out");
+    s = GSFFT_ERR_TIMEOUT;
   }
   if (taps) cudaFree(taps);
   cudaFree(tbm);

@@ -72,6 +72,7 @@ def test_cutoff_arguments_rejected(G):
     assert L.gsfft_cutoff(fake, 0, 1, 1, G.FP64, fake, None) == G.ERR_PARAM      # empty row
     assert L.gsfft_cutoff(fake, 100, 10, 0, G.FP64, fake, None) == G.ERR_PARAM   # no rows
     assert L.gsfft_cutoff(None, 100, 10, 1, G.FP64, fake, None) == G.ERR_PARAM
+    assert L.gsfft_cutoff(fake, 100, 10, 1, 7, fake, None) == G.ERR_PARAM         # no such precision
 
 
 def test_binding_constants_match_header(G):
