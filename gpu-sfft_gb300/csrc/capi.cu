@@ -749,7 +749,11 @@ Node *outer_loop(complex_t *d_x, int n, complex_t *d_filter_time, complex_t *d_f
   if (s == GSFFT_OK) s = gsfft_get_results(plan, nullptr, 0, &count, nullptr, 0, nullptr, nullptr);
   if (s == GSFFT_OK) {
     out = (Node *)malloc(sizeof(Node) * (count > 0 ? count : 1));
-    if (out) s = gsfft_get_results(plan, out, count, &count, nullptr, 0, nullptr, nullptr);
+    if (!out) {
+      set_last_error("outer_loop: host allocation of %d nodes failed", count);
+      s = GSFFT_ERR_ALLOC;
+    }
+    if (s == GSFFT_OK) s = gsfft_get_results(plan, out, count, &count, nullptr, 0, nullptr, nullptr);
     if (s == GSFFT_OK) *I_F += count;
   }
   if (s != GSFFT_OK && out) {
