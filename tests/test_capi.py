@@ -5,6 +5,8 @@ import ctypes as C
 
 import pytest
 
+from _cabi import check_binding
+
 
 def test_exports_every_declared_symbol(G):
     declared = G.exported_header_symbols()
@@ -98,66 +100,13 @@ def test_binding_constants_match_header(G):
         assert getattr(G, name) == int(codes["GSFFT_" + name]), name
 
 
-def _header_prototypes(path):
-    """{name: (return type, [argument types])} of the functions a C header
-    declares (comments and preprocessor lines removed)."""
-    import re
-    txt = open(path).read()
-    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    txt = re.sub(r"//.*", "", txt)
-    txt = re.sub(r"^\s*#.*$", "", txt, flags=re.M)
-    out = {}
-    for m in re.finditer(r"([A-Za-z_][\w \*]*?)\b(\w+)\s*\(([^;{}()]*)\)\s*;", txt, flags=re.S):
-        ret, name, args = " ".join(m.group(1).split()), m.group(2), m.group(3)
-        types = []
-        for a in (" ".join(x.split()) for x in args.split(",")):
-            if not a or a == "void":
-                continue
-            # drop the parameter name; keep pointer stars
-            types.append(a if a.endswith("*") else re.sub(r"\s*\b\w+$", "", a))
-        out[name] = (ret.replace(" typedef", "").strip(), types)
-    return out
-
-
-def _c_kind(t):
-    """Calling-convention class of a C type of gsfft.h."""
-    t = t.replace("const ", "").strip()
-    if "*" in t or t in ("gsfft_plan", "gsfft_batch"):
-        return "ptr"
-    return {"int": ("int", 4, True), "unsigned": ("int", 4, False),
-            "unsigned int": ("int", 4, False), "long long": ("int", 8, True),
-            "size_t": ("int", 8, False), "double": "f64", "float": "f32"}[t]
-
-
-def _ctypes_kind(t):
-    if t in (C.c_void_p, C.c_char_p) or (isinstance(t, type) and issubclass(t, C._Pointer)):
-        return "ptr"
-    if t is C.c_double:
-        return "f64"
-    if t is C.c_float:
-        return "f32"
-    return ("int", C.sizeof(t), t(-1).value < 0)
-
-
 def test_binding_signatures_match_header(G):
-    """Every function the Python binding declares has the header's argument
-    count and, per argument, the same width and signedness (or a pointer);
-    an int passed where the header says long long would leave the upper
-    half of the register undefined."""
-    protos = _header_prototypes(G.HEADER)
-    L = G.lib()
-    checked = 0
-    for name, (ret, args) in sorted(protos.items()):
-        f = getattr(L, name)
-        if f.argtypes is None:
-            continue  # not bound in Python
-        assert len(f.argtypes) == len(args), (name, args)
-        for i, (ct, pt) in enumerate(zip(args, f.argtypes)):
-            assert _c_kind(ct) == _ctypes_kind(pt), (name, i, ct, pt)
-        assert _c_kind(ret) == _ctypes_kind(f.restype), (name, ret, f.restype)
-        checked += 1
-    # the binding covers the whole header
-    assert checked == len(protos), sorted(n for n in protos if getattr(L, n).argtypes is None)
+    """Every function of include/gsfft.h is bound in Python with the header's
+    argument count and, per argument, the same width and signedness (or a
+    pointer): an int passed where the header says long long would leave the
+    upper half of the register undefined."""
+    checked, unbound = check_binding(G.lib(), G.HEADER, handles=("gsfft_plan", "gsfft_batch"))
+    assert checked == len(G.exported_header_symbols()) and not unbound, unbound
 
 
 def test_noalloc_cutoff_arguments_and_limits(G):

@@ -310,3 +310,14 @@ def test_filter_recurrence_mode_close(O):
     ft1, ff1 = O.design_filter(p, quirks=O.QUIRK_FILTER_RECURRENCE)
     assert np.abs(ff0 - ff1).max() < 1e-9
     assert np.abs(ft0 - ft1).max() < 1e-9 * np.abs(ft0).max()
+
+
+def test_oracle_binding_signatures_match_header(O):
+    """The oracle's ctypes binding passes every argument with the width and
+    signedness that oracle/sfft_oracle.h declares (void results bound as
+    None), so the checker itself cannot be fed truncated or undefined bits."""
+    from _cabi import check_binding
+    header = os.path.join(os.path.dirname(O.LIB_PATH), os.pardir, "sfft_oracle.h")
+    checked, unbound = check_binding(O.lib(), header)
+    assert checked > 0
+    assert set(unbound) <= {"oc_num_threads"}, unbound  # takes no arguments, returns int
