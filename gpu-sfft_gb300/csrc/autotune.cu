@@ -26,8 +26,10 @@ namespace {
 
 std::mutex g_cache_mu;
 
+// the flags that change a plan's pipeline, and so belong to the cache key
 constexpr unsigned kTuneFlags = GSFFT_FLAG_QUIRK_RESIDUE | GSFFT_FLAG_RAW_SELECTION |
-                                GSFFT_FLAG_TC_BUCKET_FFT | GSFFT_FLAG_TC_RLFC_FFT;
+                                GSFFT_FLAG_TC_BUCKET_FFT | GSFFT_FLAG_TC_RLFC_FFT |
+                                GSFFT_FLAG_CC_BUCKET_FFT;
 
 int cache_key(const gsfft_params &p, int precision, unsigned flags, std::string *key) {
   int dev = 0;
@@ -112,7 +114,10 @@ int measure(Bench &b, const gsfft_plan_tuning &t, float *ms, gsfft_plan_tuning *
   if (s == GSFFT_OK) {
     RunCtl c;
     if (cudaMemcpy(&c, P->ctl, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess) s = GSFFT_ERR_CUDA;
-    else if (c.err) s = GSFFT_ERR_CUDA;  // a bounded device wait gave up
+    else if (c.err) {
+      set_last_error("gsfft_autotune_plan: a bounded device-side wait gave up");
+      s = GSFFT_ERR_TIMEOUT;
+    }
   }
   if (s == GSFFT_OK) {
     *ms = total / (float)b.reps;

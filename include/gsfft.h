@@ -143,9 +143,11 @@ int gsfft_plan_get_tuning(gsfft_plan plan, gsfft_plan_tuning *out);
  * each candidate the mean of `reps` runs after one warm-up run, CUDA events
  * on `stream`) and returns the fastest in *best, with its time in *best_ms.
  * cache_path (may be NULL): a text file of earlier results, keyed by the
- * device, the precision, the tensor-core flags and the plan's sizes; a hit
- * returns at once, a new result is appended.  Allocates and frees candidate
- * plans; synchronises the stream. */
+ * device, the precision, the flags that change the pipeline (residue quirk,
+ * raw selection, tensor-core and CUDA-core FFT choices) and the plan's sizes;
+ * a hit returns at once, a new result is appended.  Allocates and frees
+ * candidate plans; synchronises the stream.  GSFFT_ERR_TIMEOUT when a
+ * candidate's bounded device-side wait gave up. */
 int gsfft_autotune_plan(const gsfft_params *p, int precision, unsigned flags, const void *d_x,
                         const complex_t *d_filter_time, const complex_t *d_filter_freq,
                         const int *h_rlfc_offsets, const int *h_a, const int *h_ai, int reps,
