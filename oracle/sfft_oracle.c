@@ -231,6 +231,10 @@ static int fft_bluestein(oc_complex *x, long N, int sign) {
   return st;
 }
 
+/* Stands in for the reference's cuFFT Z2Z transforms (innerLoop.cu:144-152,
+ * the W_RLFC-point RLFC FFT; :252-256, the B-point bucket FFT): unnormalised,
+ * in place, sign -1 forward.  Bluestein covers the non-power-of-two lengths
+ * of the filter design (cuExperiment.cu:277-448). */
 int oc_fft(oc_complex *data, long N, int sign) {
   if (N <= 0) return OC_ERR_PARAM;
   if ((N & (N - 1)) == 0) return fft_pow2(data, N, sign);
@@ -405,6 +409,7 @@ void oc_cutoff_f64(const double *samples, int size, int num, int *out) {
   }
 }
 
+/* oc_cutoff_f64's rule (innerLoop.cu:551-642) on FP32 samples. */
 void oc_cutoff_f32(const float *samples, int size, int num, int *out) {
   double *d = (double *)malloc(sizeof(double) * (size_t)size);
   for (int i = 0; i < size; i++) d[i] = samples[i]; /* exact widening */
