@@ -9,7 +9,6 @@ Every engine call goes through the C ABI: the stage drop-ins with the
 reference's signatures (innerLoop.h:32-50) and the native plan API.
 """
 import ctypes as C
-import os
 import tempfile
 
 import numpy as np
