@@ -566,7 +566,8 @@ int plan_results(Plan *P, Node *h_nodes, int nodes_cap, int *I_F, Node *h_topk, 
   }
   GS_CUDA(cudaStreamSynchronize(st));
   if (c.err) {
-    set_last_error("a bounded device-side wait gave up (streaming perm+filter or tensor-core FFT)");
+    set_last_error(
+        "a bounded device-side wait gave up (streaming perm+filter, tensor-core FFT or batch voting)");
     return GSFFT_ERR_TIMEOUT;
   }
   return c.overflow ? GSFFT_ERR_CAPACITY : GSFFT_OK;

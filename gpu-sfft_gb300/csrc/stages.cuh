@@ -22,7 +22,8 @@ struct RunCtl {
   int n_topk;
   int fmax[MAX_LOOPS]; // largest permuted residue per location loop
   unsigned ticket;
-  int err;  // a bounded device-side wait gave up (streaming perm+filter)
+  int err;  // a bounded device-side wait gave up (streaming perm+filter,
+            // tensor-core FFT passes, persistent batch voting)
   int pad[2];
 };
 
